@@ -1,0 +1,408 @@
+#!/usr/bin/env python
+"""Benchmark of heatsim2's ADI Crank-Nicolson timestep on GB300: voxel-steps/s and roofline fractions.
+
+Workload (one GPU): the composite panel -- 64 x 512 x 512 computed voxels at 0.5 mm under a fixed-temperature
+ambient layer (grid 65 x 512 x 512), anisotropic composite over aluminium, three seeded delaminations, flash
+2e9 W/m^3 for the first 5 ms step, dt = 5 ms.  A "step" is one ADI timestep over the whole grid; the default
+K = 1000 steps is the whole simulated job (t = 0 .. 5 s), timed from t = 0 after W warm-up steps on a
+throw-away copy.  Synthetic, seeded input (heatsim2_gb300.workloads.composite_panel(seed=1)).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line.  ``value`` counts computed voxels (64*512*512) per second with the state resident in
+HBM; ``e2e`` is the same metric through the C ABI with host buffers (host->device copy of T, the step,
+device->host copy of T, every step); ``roofline`` is the dominant sweep kernel against the measured HBM copy
+bandwidth; ``fp64_roofline`` the whole step against the measured FP64 FMA rate, the resource that binds;
+``cpu_baseline`` the reference (or, where it cannot be built, the oracle) on the host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "voxel-steps/s"
+SEED = 1
+# algorithmic bytes and FP64 operations per grid voxel, per kernel (dense coefficient layout, no source active):
+#   sweep_x  reads T and 9 coefficient arrays (wc wxl wxh wyl wyh wzl wzh a0 b0), writes W0
+#   sweep_y  reads W0, a1, b1, writes W1
+#   sweep_z  reads W1, a2, b2, T, writes T'
+BYTES_PER_VOXEL = {"sweep_x": 8 + 9 * 8 + 8, "sweep_y": 4 * 8, "sweep_z": 5 * 8}
+FP64_OPS_PER_VOXEL = {"sweep_x": 9, "sweep_y": 2, "sweep_z": 3}
+KERNELS = ("sweep_x", "sweep_y", "sweep_z")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--shape", type=int, nargs=3, default=[64, 512, 512], metavar=("NZ", "NY", "NX"),
+                    help="computed voxels (an ambient layer is added on top)")
+    ap.add_argument("--e2e-steps", type=int, default=30)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-worker", default=None, help=argparse.SUPPRESS)
+    return ap.parse_args()
+
+
+def workload(shape, nsteps):
+    from heatsim2_gb300 import workloads as W
+    nz, ny, nx = shape
+    wr = (min(10, ny, nx), min(60, ny, nx))
+    dr = (min(4, nz - 1), min(40, nz - 1))
+    return W.composite_panel(seed=SEED, nz=nz, ny=ny, nx=nx, nsteps=nsteps, width_range=wr, depth_range=dr)
+
+
+def read_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def read_traffic():
+    """DRAM bytes per grid voxel per launch measured by ncu (profiles/dram_traffic.txt), or {}."""
+    out = {}
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    try:
+        with open(path) as fh:
+            for line in fh:
+                parts = line.split()
+                if len(parts) >= 2 and not line.startswith("#"):
+                    out[parts[0]] = float(parts[1])
+    except OSError:
+        pass
+    return out
+
+
+class ClockSampler(object):
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active," \
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------------------------------------------------------
+# CPU baseline (the reference built in oracle/_ref, else the oracle) -- a bounded sample, own process
+# ------------------------------------------------------------------------------------------------------------
+CPU_SAMPLE_SHAPE = (64, 64, 64)
+
+
+def _cpu_impl():
+    import build_ref
+    if build_ref.available():
+        try:
+            return "reference", build_ref.import_reference()
+        except Exception:
+            pass
+    import oracle
+    from oracle_shim import HS
+    return "port", (oracle, HS)
+
+
+def cpu_worker(kind_req, seconds, max_steps, barrier=None, result=None):
+    """Time one CPU implementation on the composite panel at CPU_SAMPLE_SHAPE; returns a dict."""
+    import contextlib
+    import io
+    from heatsim2_gb300 import workloads as W
+    kind, impl = _cpu_impl()
+    spec = workload(CPU_SAMPLE_SHAPE, max_steps)
+    if kind == "reference":
+        hsr = impl
+        with contextlib.redirect_stdout(io.StringIO()):
+            P, S = hsr.setup(*W.setup_args(hsr, spec))
+        step = lambda t, T: hsr.run_adi_steps(P, S, t, spec["dt"], T, spec["arrays"]["volumetric"], vol)
+        vol = W.volumetric_tuple(hsr, spec)
+    else:
+        orc, HS = impl
+        P, _ = orc.setup(*W.setup_args(HS, spec))
+        vol = W.volumetric_tuple(HS, spec)
+        step = lambda t, T: orc.run_adi_steps(P, None, t, spec["dt"], T, spec["arrays"]["volumetric"], vol)
+    T = W.initial_temperature(spec)
+    times = W.step_times(spec, max_steps)
+    T = step(times[0], T)          # warm-up (first step)
+    if barrier is not None:
+        barrier.wait()
+    t0 = time.perf_counter()
+    n = 0
+    for t in times[1:]:
+        T = step(t, T)
+        n += 1
+        if seconds and time.perf_counter() - t0 >= seconds:
+            break
+    el = time.perf_counter() - t0
+    nz, ny, nx = CPU_SAMPLE_SHAPE
+    out = {"kind": kind, "steps": n, "seconds": el, "voxels": nz * ny * nx,
+           "value": nz * ny * nx * n / el if el > 0 else 0.0}
+    if result is not None:
+        result.put(out)
+    return out
+
+
+def run_cpu_baseline(seconds):
+    cmd = [sys.executable, os.path.abspath(__file__), "--cpu-worker", "auto", "--cpu-seconds", str(seconds)]
+    try:
+        out = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
+        d = json.loads(out.stdout.strip().splitlines()[-1])
+    except Exception as e:
+        return {"value": None, "unit": METRIC, "cores": 1, "kind": "port", "sample": "failed: %s" % (e,)}
+    nz, ny, nx = CPU_SAMPLE_SHAPE
+    return {"value": d["value"], "unit": METRIC, "cores": 1, "kind": d["kind"],
+            "sample": "composite panel %dx%dx%d (+ambient layer), %d steps after setup, %.1f s, 1 thread "
+                      "(the reference is single-threaded); cpu: %s" % (nz, ny, nx, d["steps"], d["seconds"],
+                                                                     cpu_model())}
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip() + " x%d" % os.cpu_count()
+    except OSError:
+        pass
+    return "%d cores" % os.cpu_count()
+
+
+# ------------------------------------------------------------------------------------------------------------
+# reference arm: the reference CPU implementation on all host cores (one process per core)
+# ------------------------------------------------------------------------------------------------------------
+def reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    nproc = os.cpu_count() or 1
+    barrier = ctx.Barrier(nproc)
+    q = ctx.Queue()
+    steps = max(1, args.steps)
+    procs = [ctx.Process(target=cpu_worker, args=("auto", 0.0, steps + 1, barrier, q)) for _ in range(nproc)]
+    for p in procs:
+        p.start()
+    res = [q.get() for _ in procs]
+    for p in procs:
+        p.join()
+    el = max(r["seconds"] for r in res)
+    total = sum(r["voxels"] * r["steps"] for r in res)
+    value = total / el
+    nz, ny, nx = CPU_SAMPLE_SHAPE
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+        "steps": steps, "warmup": 1, "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "composite panel %dx%dx%d (+ambient), one independent instance per host core"
+                               % (nz, ny, nx), "processes": nproc},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": nproc, "kind": res[0]["kind"],
+                         "sample": "%d processes x %d steps of the composite panel %dx%dx%d after setup; cpu: %s"
+                                   % (nproc, steps, nz, ny, nx, cpu_model())},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------------------------
+def gpu_arm(args, world, rank, local_rank):
+    import ctypes
+    import numpy as np
+    import torch
+    import heatsim2_gb300 as hs
+    from heatsim2_gb300 import _native, workloads as W
+    from heatsim2_gb300.alternatingdirection import _ClassSources, source_table
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    L = _native.load()
+    K, Wm = args.steps, args.warmup
+    spec = workload(args.shape, K)
+    t0 = time.perf_counter()
+    P, S = hs.setup(*W.setup_args(hs, spec))
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    nz, ny, nx = spec["grid"]["nz"], spec["grid"]["ny"], spec["grid"]["nx"]
+    grid_vox = nz * ny * nx
+    compute_vox = spec["compute_voxels"]
+    src = _ClassSources(W.volumetric_tuple(hs, spec))
+    times = W.step_times(spec, max(K, Wm))
+    qtabs = np.zeros((len(times), _native.MAX_CLASSES))
+    for s, t in enumerate(times):
+        qtabs[s], _ = source_table(src, t, spec["dt"], P.volume_array)
+    T0 = torch.from_numpy(W.initial_temperature(spec)).to(dev)
+    T = T0.clone()
+    stream = torch.cuda.Stream(device=dev)
+    h = P.handle.ptr
+    _native.check(L.hs2g_set_stream(h, ctypes.c_void_p(stream.cuda_stream)))
+    kms = np.zeros(4)
+    # warm-up on a throw-away state
+    qw = np.ascontiguousarray(qtabs[:Wm])
+    _native.check(L.hs2g_run_timed(h, Wm, T0.data_ptr(), T.data_ptr(), qw.ctypes.data, _native.DEVICE,
+                                   kms.ctypes.data))
+    fma_rate = ctypes.c_double(0.0)
+    _native.check(L.hs2g_fp64_fma_rate(local_rank, ctypes.byref(fma_rate)))
+    # timed region: K steps from t = 0
+    T.copy_(T0)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    time.sleep(0.3)
+    qk = np.ascontiguousarray(qtabs[:K])
+    _native.check(L.hs2g_run_timed(h, K, T.data_ptr(), T.data_ptr(), qk.ctypes.data, _native.DEVICE,
+                                   kms.ctypes.data))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = float(kms[3])
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * compute_vox * K / (total_ms * 1e-3)
+    per_kernel_ms = {k: float(kms[i]) / K for i, k in enumerate(KERNELS)}
+    # roofline of the dominant kernel
+    hbm_peak, peak_src = read_peaks()
+    dom = max(per_kernel_ms, key=per_kernel_ms.get)
+    achieved_gbs = BYTES_PER_VOXEL[dom] * grid_vox / (per_kernel_ms[dom] * 1e-3) / 1e9
+    traffic = read_traffic()
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved_gbs / hbm_peak, "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic_bytes_per_launch": BYTES_PER_VOXEL[dom] * grid_vox,
+                "traffic": traffic[dom] * grid_vox if dom in traffic else None}
+    step_ops = sum(FP64_OPS_PER_VOXEL.values()) * grid_vox
+    fp64 = {"bound": "fp64", "achieved": step_ops / (total_ms * 1e-3 / K) / 1e12,
+            "peak": fma_rate.value / 1e12, "unit": "TFMA/s", "ops_per_voxel_step": sum(FP64_OPS_PER_VOXEL.values()),
+            "peak_source": "measured (hs2g_fp64_fma_rate, register-only FMA chains)"}
+    fp64["frac"] = fp64["achieved"] / fp64["peak"] if fp64["peak"] else None
+    per_kernel_fp64 = {k: FP64_OPS_PER_VOXEL[k] * grid_vox / (per_kernel_ms[k] * 1e-3) / fma_rate.value
+                       for k in KERNELS}
+    per_kernel_hbm = {k: BYTES_PER_VOXEL[k] * grid_vox / (per_kernel_ms[k] * 1e-3) / 1e9 / hbm_peak
+                      for k in KERNELS}
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        E = max(2, min(args.e2e_steps, K))
+        hin = torch.from_numpy(W.initial_temperature(spec)).pin_memory()
+        hout = torch.empty_like(hin).pin_memory()
+        _native.check(L.hs2g_set_stream(h, None))
+        for s in range(2):
+            _native.check(L.hs2g_step(h, hin.data_ptr(), hout.data_ptr(), qtabs[s].ctypes.data, None, None, 0))
+        hin.copy_(torch.from_numpy(W.initial_temperature(spec)))
+        te = time.perf_counter()
+        a, b = hin, hout
+        for s in range(E):
+            _native.check(L.hs2g_step(h, a.data_ptr(), b.data_ptr(), qtabs[s % len(qtabs)].ctypes.data, None, None,
+                                      0))
+            a, b = b, a
+        el = time.perf_counter() - te
+        e2e = {"value": world * compute_vox * E / el, "unit": METRIC, "h2d_bytes_per_step": grid_vox * 8,
+               "d2h_bytes_per_step": grid_vox * 8, "steps": E,
+               "path": "hs2g_step with pinned host buffers (copy in, 3 sweeps, copy out, sync) per step"}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = run_cpu_baseline(args.cpu_seconds)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K, "warmup": Wm,
+            "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "composite panel %dx%dx%d computed voxels (+1 fixed ambient layer), 0.5 mm, "
+                                   "anisotropic composite over aluminium, 3 delaminations, flash at t=0, dt=5 ms"
+                                   % tuple(args.shape),
+                       "grid": [nz, ny, nx], "computed_voxels": compute_vox, "seed": SEED,
+                       "l2": "inputs larger than L2 (T %.0f MB + step coefficients %.0f MB)"
+                             % (grid_vox * 8 / 1e6, grid_vox * 8 * 14 / 1e6),
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": roofline, "fp64_roofline": fp64,
+            "kernel_ms_per_step": per_kernel_ms, "kernel_fp64_frac": per_kernel_fp64,
+            "kernel_hbm_frac": per_kernel_hbm,
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * K, "clocks": clk, "setup_s": setup_s,
+            "device_bytes": P.device_bytes,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.cpu_worker:
+        print(json.dumps(cpu_worker(args.cpu_worker, args.cpu_seconds, 100000)), flush=True)
+        return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+        return
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    gpu_arm(args, world, rank, local_rank)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,309 @@
+"""``run_adi_steps``: one ADI Crank-Nicolson timestep on the GPU, and the objects ``setup`` returns.
+
+Mirrors ``heatsim2.alternatingdirection_c_pyx.run_adi_steps`` (reference alternatingdirection_c_pyx.pyx:287-416):
+same arguments, a fresh array returned, the source classes evaluated at ``t`` with ``dt``
+(pyx:294-386), the step's coefficients fixed by ``setup``'s dt.  ``Tarray`` may be a numpy array (copied to
+and from the device each call) or a float64 CUDA ``torch.Tensor`` on the problem's device (no copies; the
+result is a new tensor).  ``run`` advances many steps on the device in one call.
+"""
+import ctypes
+import numbers
+
+import numpy as np
+
+from . import _native
+
+NO_SOURCE = 0
+IMPULSE_SOURCE = 1
+STEPPED_SOURCE = 2
+IMPULSE_POINT_SOURCE_JOULES = 3
+SPATIALLY_Z_DECAYING_TEMPORAL_IMPULSE = 4
+
+
+class adi_params(object):
+    """Compiled problem (the reference's ADI_params, alternatingdirection_c_pyx.pyx:75-85): ``shape``,
+    ``volume_array`` (cell volume), plus the device handle that owns the step coefficients."""
+
+    shape = None
+    volume_array = None
+
+    def __init__(self, **kwargs):
+        for key, val in kwargs.items():
+            setattr(self, key, val)
+
+    @property
+    def device_bytes(self):
+        return int(_native.load().hs2g_device_bytes(self.handle.ptr))
+
+    def faces(self):
+        """(Gz, Gy, Gx, capacity, fixed) as compiled: per-face conductances (W/m^3/K), rho*c/dt per voxel
+        (1 for fixed voxels) and the fixed-temperature mask."""
+        nz, ny, nx = self.shape
+        Gz = np.empty((nz + 1, ny, nx))
+        Gy = np.empty((nz, ny + 1, nx))
+        Gx = np.empty((nz, ny, nx + 1))
+        M = np.empty((nz, ny, nx))
+        fixed = np.empty((nz, ny, nx), dtype=np.uint8)
+        L = _native.load()
+        _native.check(L.hs2g_get_faces(self.handle.ptr, Gz.ctypes.data, Gy.ctypes.data, Gx.ctypes.data,
+                                       M.ctypes.data, fixed.ctypes.data))
+        return Gz, Gy, Gx, M, fixed
+
+
+class adi_step(object):
+    """One ADI stage (the reference's pyadi_step, alternatingdirection_c_pyx.pyx:120-284): stage ``stepnum``
+    solves along the last axis of ``permuteorder``.  ``Amat``, ``Bmat``, ``Cmats``, ``Dvec``, ``Lmat`` and
+    ``Umat`` are rebuilt on demand from the compiled face conductances in the reference's matrix form (rows in
+    the permuted order), for inspection; the timestep itself never uses them."""
+
+    def __init__(self, params, permuteorder, stepnum):
+        self.ADI_params = params
+        self.permuteorder = tuple(permuteorder)
+        inv = [0, 0, 0]
+        for ind, pord in enumerate(permuteorder):
+            inv[pord] = ind
+        self.invpermuteorder = tuple(inv)
+        self.permutedshape = [params.shape[i] for i in permuteorder]
+        self.stepnum = stepnum
+        self._mats = None
+
+    def _build(self):
+        if self._mats is None:
+            from .introspect import stage_matrices
+            self._mats = stage_matrices(self.ADI_params, self.stepnum)
+        return self._mats
+
+    Amat = property(lambda self: self._build()["A"])
+    Bmat = property(lambda self: self._build()["B"])
+    Cmats = property(lambda self: self._build()["C"])
+    Dvec = property(lambda self: self._build()["D"])
+    Lmat = property(lambda self: self._build()["L"])
+    Umat = property(lambda self: self._build()["U"])
+
+
+# --------------------------------------------------------------------------------------------------------
+# sources
+# --------------------------------------------------------------------------------------------------------
+class _ClassSources(object):
+    """The class-uniform sources of a ``volumetric`` tuple, packed for hs2g_source_table."""
+
+    def __init__(self, volumetric):
+        n = len(volumetric)
+        if n > _native.MAX_CLASSES:
+            raise ValueError("at most 256 source classes")
+        self.kind = np.zeros(max(n, 1), dtype=np.int32)
+        self.params = np.zeros((max(n, 1), 4))
+        self.dense = []                     # (class index, source tuple) evaluated per voxel on the host
+        for c, src in enumerate(volumetric):
+            k = src[0]
+            if k in (NO_SOURCE, IMPULSE_SOURCE, STEPPED_SOURCE):
+                self.kind[c] = k
+                vals = [float(v) for v in src[1:]]
+                self.params[c, :len(vals)] = vals
+            elif k == IMPULSE_POINT_SOURCE_JOULES:
+                if isinstance(src[2], numbers.Number):
+                    self.kind[c] = k
+                    self.params[c, :2] = (float(src[1]), float(src[2]))
+                else:
+                    self.kind[c] = NO_SOURCE
+                    self.dense.append((c, src))
+            elif k == SPATIALLY_Z_DECAYING_TEMPORAL_IMPULSE:
+                self.kind[c] = NO_SOURCE
+                self.dense.append((c, src))
+            else:
+                raise ValueError("unknown volumetric source kind %r (class %d)" % (k, c))
+        self.n = n
+
+
+def _dense_source(shape, volume, t, dt, volumetric_elements, dense):
+    """Per-voxel source field for the sources that are not uniform over their class (pyx:307-384), or None
+    when none of them fires at t."""
+    q = None
+    for idx, src in dense:
+        kind = src[0]
+        if kind == IMPULSE_POINT_SOURCE_JOULES:
+            if t == src[1]:
+                if q is None:
+                    q = np.zeros(shape)
+                q[volumetric_elements == idx] = src[2] / (volume * dt)
+        else:
+            (_, t_imp, direc, offset, zgrid, ddz, jpm2, length) = src
+            if t == t_imp:
+                direc = np.asarray(direc, dtype="d")
+                if not ((direc == np.array([1.0, 0.0, 0.0])).all() or (direc == np.array([-1.0, 0.0, 0.0])).all()):
+                    raise AssertionError("decay direction must be +z or -z")
+                length = float(length)
+                if not length > 0:
+                    raise AssertionError("characteristic length must be positive")
+                if q is None:
+                    q = np.zeros(shape)
+                sel = volumetric_elements == idx
+                centre = zgrid * direc[0] - float(offset)
+                ddz = abs(float(ddz))
+                left = centre - ddz / 2.0
+                right = centre + ddz / 2.0
+                use = sel & (right > 0.0)
+                r = right[use]
+                lft = left[use]
+                lft[lft < 0.0] = 0.0
+                # fraction of a (1/l) exp(-d/l) profile deposited between the cell's z boundaries
+                frac = -np.exp(-r / length) + np.exp(-lft / length)
+                q[use] = frac * float(jpm2) / (ddz * dt)
+    return q
+
+
+def source_table(sources, t, dt, volume):
+    """(qtab ndarray[256], any_active) for the class-uniform sources at time t."""
+    qtab = np.zeros(_native.MAX_CLASSES)
+    L = _native.load()
+    active = _native.check(L.hs2g_source_table(sources.n, sources.kind.ctypes.data, sources.params.ctypes.data,
+                                               float(t), float(dt), float(volume), qtab.ctypes.data))
+    return qtab, active > 0
+
+
+# --------------------------------------------------------------------------------------------------------
+# stepping
+# --------------------------------------------------------------------------------------------------------
+def _is_torch_cuda(x):
+    try:
+        import torch
+    except ImportError:
+        return False
+    return isinstance(x, torch.Tensor) and x.is_cuda
+
+
+def _class_map_update(P, volumetric_elements):
+    """The host source-class map to upload when it differs from the one on the device, else None."""
+    if volumetric_elements is None or volumetric_elements is P.compiled_volumetric:
+        return None
+    ve = np.ascontiguousarray(volumetric_elements, dtype=np.uint8)
+    if ve.shape != tuple(P.shape):
+        raise ValueError("volumetric_elements has shape %s, expected %s" % (ve.shape, tuple(P.shape)))
+    if np.array_equal(ve, P.compiled_volumetric):
+        return None
+    P.compiled_volumetric = ve.copy()
+    return P.compiled_volumetric
+
+
+def run_adi_steps(ADI_params, ADI_steps, t, dt, Tarray, volumetric_elements, volumetric):
+    """Advance ``Tarray`` by one timestep; returns a new array (numpy in, numpy out; CUDA tensor in, tensor out)."""
+    P = ADI_params
+    L = _native.load()
+    sources = _ClassSources(volumetric)
+    qtab, active = source_table(sources, t, dt, P.volume_array)
+    ve = volumetric_elements
+    qdense = _dense_source(P.shape, P.volume_array, t, dt, np.asarray(ve), sources.dense) if sources.dense else None
+    newmap = _class_map_update(P, ve) if active else None
+    qptr = qtab.ctypes.data if active else None
+    if _is_torch_cuda(Tarray):
+        import torch
+        T = Tarray
+        if T.dtype != torch.float64:
+            raise ValueError("Tarray must be float64")
+        if tuple(T.shape) != tuple(P.shape):
+            raise ValueError("Tarray has shape %s, expected %s" % (tuple(T.shape), tuple(P.shape)))
+        if T.device.index != P.device:
+            raise ValueError("Tarray is on cuda:%d, the problem on cuda:%d" % (T.device.index, P.device))
+        T = T.contiguous()
+        out = torch.empty_like(T)
+        qd = None
+        if qdense is not None:
+            qd = torch.from_numpy(qdense).to(T.device)
+        stream = torch.cuda.current_stream(T.device)
+        _native.check(L.hs2g_set_stream(P.handle.ptr, ctypes.c_void_p(stream.cuda_stream)))
+        _native.check(L.hs2g_step(P.handle.ptr, T.data_ptr(), out.data_ptr(), qptr,
+                                  qd.data_ptr() if qd is not None else None,
+                                  newmap.ctypes.data if newmap is not None else None, _native.DEVICE))
+        if qd is not None:
+            qd.record_stream(stream)
+        return out
+    T = np.ascontiguousarray(Tarray, dtype="d")
+    if T.shape != tuple(P.shape):
+        raise ValueError("Tarray has shape %s, expected %s" % (T.shape, tuple(P.shape)))
+    out = np.empty_like(T)
+    _native.check(L.hs2g_set_stream(P.handle.ptr, None))
+    _native.check(L.hs2g_step(P.handle.ptr, T.ctypes.data, out.ctypes.data, qptr,
+                              qdense.ctypes.data if qdense is not None else None,
+                              newmap.ctypes.data if newmap is not None else None, 0))
+    return out
+
+
+def run(ADI_params, Tarray, times, dt, volumetric_elements, volumetric, record_layer=None):
+    """Advance ``Tarray`` through one step per value in ``times`` (the t passed to each step), on the device.
+
+    Equivalent to calling run_adi_steps once per t, but steps without per-voxel sources are queued in one
+    native call.  Returns ``T`` (or ``(T, history)`` with ``record_layer``: the layer z=record_layer after every
+    step, shape (len(times), ny, nx))."""
+    P = ADI_params
+    L = _native.load()
+    sources = _ClassSources(volumetric)
+    nz, ny, nx = P.shape
+    times = [float(t) for t in times]
+    n = len(times)
+    on_dev = _is_torch_cuda(Tarray)
+    if on_dev:
+        import torch
+        T = Tarray.contiguous().clone()
+        hist = torch.empty((n, ny, nx), dtype=torch.float64, device=T.device) if record_layer is not None else None
+        stream = torch.cuda.current_stream(T.device)
+        _native.check(L.hs2g_set_stream(P.handle.ptr, ctypes.c_void_p(stream.cuda_stream)))
+        ptr = T.data_ptr()
+        flags = _native.DEVICE
+    else:
+        T = np.ascontiguousarray(Tarray, dtype="d").copy()
+        hist = np.empty((n, ny, nx)) if record_layer is not None else None
+        _native.check(L.hs2g_set_stream(P.handle.ptr, None))
+        ptr = T.ctypes.data
+        flags = 0
+    ve = np.asarray(volumetric_elements)
+    qtabs = np.zeros((n, _native.MAX_CLASSES))
+    dense_steps = {}
+    any_active = False
+    for s, t in enumerate(times):
+        qtabs[s], act = source_table(sources, t, dt, P.volume_array)
+        any_active |= act
+        if sources.dense:
+            qd = _dense_source(P.shape, P.volume_array, t, dt, ve, sources.dense)
+            if qd is not None:
+                dense_steps[s] = qd
+    # a changed source-class map is uploaded with the first step (run on its own for that reason)
+    newmap = _class_map_update(P, ve) if (any_active or dense_steps) else None
+    s = 0
+    first = True
+    while s < n:
+        if s in dense_steps or (first and newmap is not None):
+            qd = dense_steps.get(s)
+            if on_dev and qd is not None:
+                qd = torch.from_numpy(qd).to(T.device)
+                qdp = qd.data_ptr()
+            else:
+                qdp = qd.ctypes.data if qd is not None else None
+            _native.check(L.hs2g_step(P.handle.ptr, ptr, ptr, qtabs[s].ctypes.data, qdp,
+                                      newmap.ctypes.data if (first and newmap is not None) else None,
+                                      flags | _native.SYNC))
+            if hist is not None:
+                hist[s] = T[record_layer]
+            s += 1
+            first = False
+            continue
+        e = s
+        while e < n and e not in dense_steps:
+            e += 1
+        chunk = np.ascontiguousarray(qtabs[s:e])
+        if hist is not None:
+            hptr = hist[s:e].data_ptr() if on_dev else np.ascontiguousarray(hist[s:e]).ctypes.data
+            if on_dev:
+                _native.check(L.hs2g_run(P.handle.ptr, e - s, ptr, ptr, chunk.ctypes.data, int(record_layer), hptr,
+                                         flags))
+            else:
+                hbuf = np.empty((e - s, ny, nx))
+                _native.check(L.hs2g_run(P.handle.ptr, e - s, ptr, ptr, chunk.ctypes.data, int(record_layer),
+                                         hbuf.ctypes.data, flags))
+                hist[s:e] = hbuf
+        else:
+            _native.check(L.hs2g_run(P.handle.ptr, e - s, ptr, ptr, chunk.ctypes.data, 0, None, flags))
+        s = e
+        first = False
+    if on_dev:
+        stream.synchronize()
+    return (T, hist) if record_layer is not None else T

@@ -1,0 +1,630 @@
+// C ABI of the hs2g library (declared in include/hs2g.h).  Host-side runtime: owns device buffers, compiles a
+// problem into step coefficients and queues timesteps on a stream.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "hs2g_internal.cuh"
+
+using hs2g::Coeffs;
+using hs2g::Dims;
+
+struct hs2g_handle {
+  int device = 0;
+  Dims d{0, 0, 0};
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  // compiled problem (device)
+  double* Gz = nullptr;
+  double* Gy = nullptr;
+  double* Gx = nullptr;
+  double* M = nullptr;
+  uint8_t* compute = nullptr;
+  uint8_t* vclass = nullptr;
+  double* coef_block = nullptr;
+  Coeffs c{};
+  // per-step scratch (device)
+  double* W0 = nullptr;
+  double* W1 = nullptr;
+  // staging for host-pointer calls (device), allocated on first use
+  double* Tin_dev = nullptr;
+  double* Tout_dev = nullptr;
+  double* qdense_dev = nullptr;
+  double* hist_dev = nullptr;
+  int64_t hist_len = 0;
+  unsigned long long* err_dev = nullptr;
+  int64_t bytes = 0;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(HS2G_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+#define HS2G_CUDA(call, what)                          \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+// Restores the caller's current device on scope exit, so that calls into the library leave torch's (or any
+// other runtime user's) device selection unchanged.
+struct DeviceGuard {
+  int prev = -1;
+  bool ok = false;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    ok = (prev == dev) || (cudaSetDevice(dev) == cudaSuccess);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+template <typename T>
+int dalloc(hs2g_handle* h, T** p, int64_t count, const char* what) {
+  const size_t bytes = (size_t)(count > 0 ? count : 1) * sizeof(T);
+  cudaError_t e = cudaMalloc((void**)p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return fail(HS2G_ERR_NOMEM, "cudaMalloc of %zu bytes for %s failed: %s", bytes, what, cudaGetErrorString(e));
+  }
+  h->bytes += (int64_t)bytes;
+  return HS2G_OK;
+}
+
+template <typename T>
+void dfree(hs2g_handle* h, T*& p, int64_t count) {
+  if (p) {
+    cudaFree(p);
+    h->bytes -= (int64_t)(count > 0 ? count : 1) * (int64_t)sizeof(T);
+  }
+  p = nullptr;
+}
+
+const char* axis_name(int axis) { return axis == 0 ? "z" : axis == 1 ? "y" : axis == 2 ? "x" : "voxel"; }
+
+int check_kernel_error(hs2g_handle* h) {
+  unsigned long long v = 0;
+  HS2G_CUDA(cudaMemcpyAsync(&v, h->err_dev, sizeof(v), cudaMemcpyDeviceToHost, h->stream), "read error word");
+  HS2G_CUDA(cudaStreamSynchronize(h->stream), "compile");
+  if (!v) return HS2G_OK;
+  const int code = -(int)(v >> 56);
+  const int axis = (int)((v >> 54) & 3);
+  const int64_t idx = (int64_t)(v & ((1ull << 54) - 1));
+  const Dims& d = h->d;
+  int64_t fz = d.nz, fy = d.ny, fx = d.nx;
+  if (axis == 0) fz += 1;
+  if (axis == 1) fy += 1;
+  if (axis == 2) fx += 1;
+  const int64_t i = idx % fx, j = (idx / fx) % fy, k = idx / (fx * fy);
+  const char* what = "invalid problem";
+  switch (code) {
+    case HS2G_ERR_EXTERIOR:
+      what = "a computed voxel has a non-insulating face on the exterior of the grid (the reference would read "
+             "outside the domain); set exterior faces to an insulating class";
+      break;
+    case HS2G_ERR_KTYPE:
+      what = "a boundary class uses the conductivity in a form the material does not have (scalar boundary "
+             "class with a matrix k, or an indexed one with a scalar k)";
+      break;
+    case HS2G_ERR_UNALIGNED:
+      what = "a face flux couples temperatures across axes: anisotropy not aligned with the grid axes "
+             "(unaligned_anisotropic) is not supported";
+      break;
+    case HS2G_ERR_FORM:
+      what = "a face flux is not a conservative two-point difference inside a Crank-Nicolson group()";
+      break;
+    case HS2G_ERR_CAPACITY:
+      what = "a computed voxel has rho*c/dt <= 0 or not finite";
+      break;
+    case HS2G_ERR_ARG:
+      what = "a class index is out of range of the materials / boundaries tuple, or a value is not finite";
+      break;
+  }
+  return fail(code, "%s (at %s index [%lld,%lld,%lld])", what, axis_name(axis), (long long)k, (long long)j,
+              (long long)i);
+}
+
+int alloc_common(hs2g_handle* h) {
+  const int64_t n = h->d.nvox();
+  int rc;
+  if ((rc = dalloc(h, &h->Gz, (h->d.nz + 1) * h->d.nxy(), "Gz"))) return rc;
+  if ((rc = dalloc(h, &h->Gy, h->d.nz * (h->d.ny + 1) * h->d.nx, "Gy"))) return rc;
+  if ((rc = dalloc(h, &h->Gx, h->d.nz * h->d.ny * (h->d.nx + 1), "Gx"))) return rc;
+  if ((rc = dalloc(h, &h->M, n, "capacity"))) return rc;
+  if ((rc = dalloc(h, &h->compute, n, "compute mask"))) return rc;
+  if ((rc = dalloc(h, &h->vclass, n, "source classes"))) return rc;
+  if ((rc = dalloc(h, &h->W0, n, "stage buffer 0"))) return rc;
+  if ((rc = dalloc(h, &h->W1, n, "stage buffer 1"))) return rc;
+  if ((rc = dalloc(h, &h->coef_block, n * hs2g::kNumCoeffArrays, "step coefficients"))) return rc;
+  if ((rc = dalloc(h, &h->err_dev, 1, "error word"))) return rc;
+  double** slots[hs2g::kNumCoeffArrays] = {&h->c.wc, &h->c.wxl, &h->c.wxh, &h->c.wyl, &h->c.wyh,
+                                           &h->c.wzl, &h->c.wzh, &h->c.wq, &h->c.a0, &h->c.b0,
+                                           &h->c.a1, &h->c.b1, &h->c.a2, &h->c.b2};
+  for (int s = 0; s < hs2g::kNumCoeffArrays; ++s) *slots[s] = h->coef_block + (int64_t)s * n;
+  HS2G_CUDA(cudaMemsetAsync(h->err_dev, 0, sizeof(unsigned long long), h->stream), "clear error word");
+  return HS2G_OK;
+}
+
+int new_handle(int device, const Dims& d, hs2g_handle** out) {
+  if (d.nz < 1 || d.ny < 1 || d.nx < 1) return fail(HS2G_ERR_ARG, "grid shape must be positive");
+  if (d.nvox() > ((int64_t)1 << 40)) return fail(HS2G_ERR_ARG, "grid too large");
+  hs2g_handle* h = new hs2g_handle();
+  h->device = device;
+  h->d = d;
+  cudaError_t e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete h;
+    return cuda_fail(e, "cudaStreamCreate");
+  }
+  h->stream = h->own_stream;
+  *out = h;
+  return HS2G_OK;
+}
+
+int factor(hs2g_handle* h) {
+  const int64_t n = h->d.nvox();
+  double *s2 = nullptr, *sigma = nullptr;
+  int rc;
+  if ((rc = dalloc(h, &s2, n, "factor scratch"))) return rc;
+  if ((rc = dalloc(h, &sigma, n, "factor scratch"))) {
+    dfree(h, s2, n);
+    return rc;
+  }
+  cudaError_t e = hs2g::launch_factor(h->d, h->Gz, h->Gy, h->Gx, h->M, h->compute, s2, sigma, h->c, h->stream);
+  cudaError_t e2 = cudaStreamSynchronize(h->stream);
+  dfree(h, s2, n);
+  dfree(h, sigma, n);
+  if (e != cudaSuccess) return cuda_fail(e, "factor kernels");
+  if (e2 != cudaSuccess) return cuda_fail(e2, "factor kernels");
+  return HS2G_OK;
+}
+
+int ensure_staging(hs2g_handle* h) {
+  const int64_t n = h->d.nvox();
+  int rc;
+  if (!h->Tin_dev && (rc = dalloc(h, &h->Tin_dev, n, "input staging"))) return rc;
+  if (!h->Tout_dev && (rc = dalloc(h, &h->Tout_dev, n, "output staging"))) return rc;
+  return HS2G_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hs2g_abi_version(void) { return HS2G_ABI_VERSION; }
+
+const char* hs2g_last_error(void) { return g_last_error.c_str(); }
+
+void hs2g_destroy(hs2g_handle* h) {
+  if (!h) return;
+  DeviceGuard g(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  const int64_t n = h->d.nvox();
+  dfree(h, h->Gz, 0);
+  dfree(h, h->Gy, 0);
+  dfree(h, h->Gx, 0);
+  dfree(h, h->M, n);
+  dfree(h, h->compute, n);
+  dfree(h, h->vclass, n);
+  dfree(h, h->coef_block, 0);
+  dfree(h, h->W0, n);
+  dfree(h, h->W1, n);
+  dfree(h, h->Tin_dev, n);
+  dfree(h, h->Tout_dev, n);
+  dfree(h, h->qdense_dev, n);
+  dfree(h, h->hist_dev, 0);
+  dfree(h, h->err_dev, 1);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  delete h;
+}
+
+int hs2g_create_classes(const hs2g_class_problem* p, int device, hs2g_handle** out) {
+  if (!p || !out) return fail(HS2G_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (!p->materials || !p->forms || !p->material || !p->boundary_z || !p->boundary_y || !p->boundary_x)
+    return fail(HS2G_ERR_ARG, "null array in problem");
+  if (p->nmat < 1 || p->nmat > HS2G_MAX_CLASSES || p->nbnd < 1 || p->nbnd > HS2G_MAX_CLASSES)
+    return fail(HS2G_ERR_ARG, "material / boundary class count must be in 1..256");
+  for (int b = 0; b < p->nbnd * 3; ++b)
+    if (p->forms[b].nzero < 0 || p->forms[b].nzero > HS2G_MAX_ZERO_FORMS)
+      return fail(HS2G_ERR_ARG, "boundary form %d has %d zero forms", b / 3, p->forms[b].nzero);
+  DeviceGuard g(device);
+  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", device);
+  hs2g_handle* h = nullptr;
+  int rc = new_handle(device, Dims{p->nz, p->ny, p->nx}, &h);
+  if (rc) return rc;
+  const Dims& d = h->d;
+  const int64_t n = d.nvox();
+  uint8_t *mat = nullptr, *bz = nullptr, *by = nullptr, *bx = nullptr;
+  hs2g_material* mats = nullptr;
+  hs2g_face_form* forms = nullptr;
+  auto cleanup_tmp = [&]() {
+    dfree(h, mat, n);
+    dfree(h, bz, 0);
+    dfree(h, by, 0);
+    dfree(h, bx, 0);
+    dfree(h, mats, p->nmat);
+    dfree(h, forms, p->nbnd * 3);
+  };
+  const int64_t nfz = (d.nz + 1) * d.nxy(), nfy = d.nz * (d.ny + 1) * d.nx, nfx = d.nz * d.ny * (d.nx + 1);
+  if ((rc = alloc_common(h)) || (rc = dalloc(h, &mat, n, "material classes")) ||
+      (rc = dalloc(h, &bz, nfz, "z boundary classes")) || (rc = dalloc(h, &by, nfy, "y boundary classes")) ||
+      (rc = dalloc(h, &bx, nfx, "x boundary classes")) || (rc = dalloc(h, &mats, p->nmat, "material table")) ||
+      (rc = dalloc(h, &forms, p->nbnd * 3, "boundary forms"))) {
+    std::string msg = g_last_error;
+    cleanup_tmp();
+    hs2g_destroy(h);
+    g_last_error = msg;
+    return rc;
+  }
+  cudaStream_t s = h->stream;
+  cudaError_t e = cudaSuccess;
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+  };
+  up(mat, p->material, (size_t)n);
+  up(bz, p->boundary_z, (size_t)nfz);
+  up(by, p->boundary_y, (size_t)nfy);
+  up(bx, p->boundary_x, (size_t)nfx);
+  up(mats, p->materials, sizeof(hs2g_material) * p->nmat);
+  up(forms, p->forms, sizeof(hs2g_face_form) * p->nbnd * 3);
+  if (p->volumetric)
+    up(h->vclass, p->volumetric, (size_t)n);
+  else if (e == cudaSuccess)
+    e = cudaMemsetAsync(h->vclass, 0, (size_t)n, s);
+  if (e == cudaSuccess) e = hs2g::launch_faces(d, 0, mat, bz, mats, p->nmat, forms, p->nbnd, h->Gz, h->err_dev, s);
+  if (e == cudaSuccess) e = hs2g::launch_faces(d, 1, mat, by, mats, p->nmat, forms, p->nbnd, h->Gy, h->err_dev, s);
+  if (e == cudaSuccess) e = hs2g::launch_faces(d, 2, mat, bx, mats, p->nmat, forms, p->nbnd, h->Gx, h->err_dev, s);
+  if (e == cudaSuccess)
+    e = hs2g::launch_capacity_from_classes(d, mat, mats, p->nmat, h->M, h->compute, h->err_dev, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cleanup_tmp();
+  if (e != cudaSuccess) {
+    rc = cuda_fail(e, "compile kernels");
+  } else {
+    rc = check_kernel_error(h);
+  }
+  if (!rc) rc = factor(h);
+  if (rc) {
+    std::string msg = g_last_error;
+    hs2g_destroy(h);
+    g_last_error = msg;
+    return rc;
+  }
+  *out = h;
+  return HS2G_OK;
+}
+
+int hs2g_create_dense(const hs2g_dense_problem* p, int device, hs2g_handle** out) {
+  if (!p || !out) return fail(HS2G_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (!p->Gz || !p->Gy || !p->Gx || !p->capacity) return fail(HS2G_ERR_ARG, "null array in problem");
+  DeviceGuard g(device);
+  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", device);
+  hs2g_handle* h = nullptr;
+  int rc = new_handle(device, Dims{p->nz, p->ny, p->nx}, &h);
+  if (rc) return rc;
+  const Dims& d = h->d;
+  const int64_t n = d.nvox();
+  if ((rc = alloc_common(h))) {
+    std::string msg = g_last_error;
+    hs2g_destroy(h);
+    g_last_error = msg;
+    return rc;
+  }
+  cudaStream_t s = h->stream;
+  cudaError_t e = cudaSuccess;
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+  };
+  up(h->Gz, p->Gz, sizeof(double) * (d.nz + 1) * d.nxy());
+  up(h->Gy, p->Gy, sizeof(double) * d.nz * (d.ny + 1) * d.nx);
+  up(h->Gx, p->Gx, sizeof(double) * d.nz * d.ny * (d.nx + 1));
+  up(h->M, p->capacity, sizeof(double) * n);
+  std::vector<uint8_t> comp((size_t)n, 1);
+  if (p->fixed)
+    for (int64_t v = 0; v < n; ++v) comp[(size_t)v] = p->fixed[v] ? 0 : 1;
+  up(h->compute, comp.data(), (size_t)n);
+  if (p->volumetric)
+    up(h->vclass, p->volumetric, (size_t)n);
+  else if (e == cudaSuccess)
+    e = cudaMemsetAsync(h->vclass, 0, (size_t)n, s);
+  if (e == cudaSuccess) e = hs2g::launch_validate_dense(d, h->Gz, h->Gy, h->Gx, h->M, h->compute, h->err_dev, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  rc = (e != cudaSuccess) ? cuda_fail(e, "dense compile") : check_kernel_error(h);
+  if (!rc) rc = factor(h);
+  if (rc) {
+    std::string msg = g_last_error;
+    hs2g_destroy(h);
+    g_last_error = msg;
+    return rc;
+  }
+  *out = h;
+  return HS2G_OK;
+}
+
+int hs2g_set_stream(hs2g_handle* h, void* stream) {
+  if (!h) return fail(HS2G_ERR_ARG, "null handle");
+  h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+  return HS2G_OK;
+}
+
+int hs2g_shape(const hs2g_handle* h, int64_t shape[3]) {
+  if (!h || !shape) return fail(HS2G_ERR_ARG, "null argument");
+  shape[0] = h->d.nz;
+  shape[1] = h->d.ny;
+  shape[2] = h->d.nx;
+  return HS2G_OK;
+}
+
+int64_t hs2g_device_bytes(const hs2g_handle* h) { return h ? h->bytes : 0; }
+
+int hs2g_source_table(int nsrc, const int32_t* kind, const double* params, double t, double dt, double volume,
+                      double* qtab) {
+  if (nsrc < 0 || nsrc > HS2G_MAX_CLASSES || !qtab || (nsrc > 0 && (!kind || !params)))
+    return fail(HS2G_ERR_ARG, "bad source table arguments");
+  int active = 0;
+  for (int c = 0; c < HS2G_MAX_CLASSES; ++c) qtab[c] = 0.0;
+  for (int c = 0; c < nsrc; ++c) {
+    const double* a = params + 4 * c;
+    double q = 0.0;
+    switch (kind[c]) {
+      case HS2G_NO_SOURCE:
+        break;
+      case HS2G_IMPULSE_SOURCE:  // exact time match, energy / dt (alternatingdirection_c_pyx.pyx:296-300)
+        if (t == a[0]) q = a[1] / dt;
+        break;
+      case HS2G_STEPPED_SOURCE:  // inclusive window (pyx:301-306)
+        if (t >= a[0] && t <= a[1]) q = a[2];
+        break;
+      case HS2G_IMPULSE_POINT_SOURCE_JOULES:  // joules per element / (volume * dt) (pyx:307-319)
+        if (t == a[0]) q = a[1] / (volume * dt);
+        break;
+      default:
+        return fail(HS2G_ERR_ARG, "source class %d has kind %d, which is not evaluated per class", c, kind[c]);
+    }
+    qtab[c] = q;
+    if (q != 0.0) ++active;
+  }
+  return active;
+}
+
+int hs2g_step(hs2g_handle* h, const double* T_in, double* T_out, const double* qtab, const double* qdense,
+              const uint8_t* volumetric, int flags) {
+  if (!h || !T_in || !T_out) return fail(HS2G_ERR_ARG, "null argument");
+  DeviceGuard g(h->device);
+  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", h->device);
+  const Dims& d = h->d;
+  const int64_t n = d.nvox();
+  const bool dev = (flags & HS2G_DEVICE) != 0;
+  cudaStream_t s = h->stream;
+  if (volumetric) HS2G_CUDA(cudaMemcpyAsync(h->vclass, volumetric, (size_t)n, cudaMemcpyHostToDevice, s), "upload classes");
+  hs2g::StepArgs a{};
+  a.d = d;
+  a.W0 = h->W0;
+  a.W1 = h->W1;
+  a.vclass = h->vclass;
+  hs2g::QTable q;
+  a.has_qtab = false;
+  if (qtab) {
+    for (int c = 0; c < HS2G_MAX_CLASSES; ++c) {
+      q.q[c] = qtab[c];
+      if (qtab[c] != 0.0) a.has_qtab = true;
+    }
+  } else {
+    memset(&q, 0, sizeof(q));
+  }
+  if (qdense) {
+    if (dev) {
+      a.qdense = qdense;
+    } else {
+      int rc;
+      if (!h->qdense_dev && (rc = dalloc(h, &h->qdense_dev, n, "source staging"))) return rc;
+      HS2G_CUDA(cudaMemcpyAsync(h->qdense_dev, qdense, sizeof(double) * n, cudaMemcpyHostToDevice, s),
+                "upload source field");
+      a.qdense = h->qdense_dev;
+    }
+  }
+  if (dev) {
+    a.T_in = T_in;
+    a.T_out = T_out;
+  } else {
+    int rc = ensure_staging(h);
+    if (rc) return rc;
+    HS2G_CUDA(cudaMemcpyAsync(h->Tin_dev, T_in, sizeof(double) * n, cudaMemcpyHostToDevice, s), "upload T");
+    a.T_in = h->Tin_dev;
+    a.T_out = h->Tout_dev;
+  }
+  cudaError_t e = hs2g::launch_step(a, h->c, q, s);
+  if (e != cudaSuccess) return cuda_fail(e, "step kernels");
+  if (!dev) {
+    HS2G_CUDA(cudaMemcpyAsync(T_out, h->Tout_dev, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "download T");
+    HS2G_CUDA(cudaStreamSynchronize(s), "step");
+  } else if (flags & HS2G_SYNC) {
+    HS2G_CUDA(cudaStreamSynchronize(s), "step");
+  }
+  return HS2G_OK;
+}
+
+int hs2g_run(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, const double* qtabs,
+             int record_layer, double* history, int flags) {
+  if (!h || !T_in || !T_out || nsteps < 0) return fail(HS2G_ERR_ARG, "bad argument");
+  if (history && (record_layer < 0 || record_layer >= h->d.nz))
+    return fail(HS2G_ERR_ARG, "record_layer %d outside 0..%lld", record_layer, (long long)h->d.nz - 1);
+  DeviceGuard g(h->device);
+  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", h->device);
+  const Dims& d = h->d;
+  const int64_t n = d.nvox();
+  const bool dev = (flags & HS2G_DEVICE) != 0;
+  cudaStream_t s = h->stream;
+  const double* src = T_in;
+  double* dst = T_out;
+  if (!dev) {
+    int rc = ensure_staging(h);
+    if (rc) return rc;
+    HS2G_CUDA(cudaMemcpyAsync(h->Tin_dev, T_in, sizeof(double) * n, cudaMemcpyHostToDevice, s), "upload T");
+    src = h->Tin_dev;
+    dst = h->Tout_dev;
+  }
+  double* hist = nullptr;
+  if (history) {
+    if (dev) {
+      hist = history;
+    } else {
+      const int64_t need = (int64_t)nsteps * d.nxy();
+      if (need > h->hist_len) {
+        dfree(h, h->hist_dev, h->hist_len);
+        int rc = dalloc(h, &h->hist_dev, need, "surface history");
+        if (rc) return rc;
+        h->hist_len = need;
+      }
+      hist = h->hist_dev;
+    }
+  }
+  hs2g::StepArgs a{};
+  a.d = d;
+  a.W0 = h->W0;
+  a.W1 = h->W1;
+  a.vclass = h->vclass;
+  hs2g::QTable q;
+  memset(&q, 0, sizeof(q));
+  for (int st = 0; st < nsteps; ++st) {
+    a.has_qtab = false;
+    if (qtabs) {
+      const double* qt = qtabs + (int64_t)st * HS2G_MAX_CLASSES;
+      for (int c = 0; c < HS2G_MAX_CLASSES; ++c) {
+        q.q[c] = qt[c];
+        if (qt[c] != 0.0) a.has_qtab = true;
+      }
+    }
+    a.T_in = src;
+    a.T_out = dst;
+    cudaError_t e = hs2g::launch_step(a, h->c, q, s);
+    if (e != cudaSuccess) return cuda_fail(e, "step kernels");
+    if (hist) {
+      e = hs2g::launch_copy_layer(d, dst, record_layer, hist + (int64_t)st * d.nxy(), s);
+      if (e != cudaSuccess) return cuda_fail(e, "history copy");
+    }
+    src = dst;
+  }
+  if (nsteps == 0 && src != dst) {
+    HS2G_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, s), "copy T");
+  }
+  if (!dev) {
+    HS2G_CUDA(cudaMemcpyAsync(T_out, h->Tout_dev, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "download T");
+    if (history)
+      HS2G_CUDA(cudaMemcpyAsync(history, h->hist_dev, sizeof(double) * nsteps * d.nxy(), cudaMemcpyDeviceToHost, s),
+                "download history");
+    HS2G_CUDA(cudaStreamSynchronize(s), "run");
+  } else if (flags & HS2G_SYNC) {
+    HS2G_CUDA(cudaStreamSynchronize(s), "run");
+  }
+  return HS2G_OK;
+}
+
+int hs2g_run_timed(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, const double* qtabs, int flags,
+                   double* kernel_ms) {
+  if (!h || !T_in || !T_out || nsteps < 0 || !kernel_ms) return fail(HS2G_ERR_ARG, "bad argument");
+  if (!(flags & HS2G_DEVICE)) return fail(HS2G_ERR_ARG, "hs2g_run_timed takes device pointers");
+  DeviceGuard g(h->device);
+  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", h->device);
+  cudaStream_t s = h->stream;
+  std::vector<cudaEvent_t> ev((size_t)nsteps * 4);
+  for (auto& e : ev) HS2G_CUDA(cudaEventCreate(&e), "cudaEventCreate");
+  hs2g::StepArgs a{};
+  a.d = h->d;
+  a.W0 = h->W0;
+  a.W1 = h->W1;
+  a.vclass = h->vclass;
+  hs2g::QTable q;
+  memset(&q, 0, sizeof(q));
+  const double* src = T_in;
+  int rc = HS2G_OK;
+  for (int st = 0; st < nsteps && rc == HS2G_OK; ++st) {
+    a.has_qtab = false;
+    if (qtabs) {
+      const double* qt = qtabs + (int64_t)st * HS2G_MAX_CLASSES;
+      for (int c = 0; c < HS2G_MAX_CLASSES; ++c) {
+        q.q[c] = qt[c];
+        if (qt[c] != 0.0) a.has_qtab = true;
+      }
+    }
+    a.T_in = src;
+    a.T_out = T_out;
+    cudaError_t e = hs2g::launch_step_events(a, h->c, q, s, &ev[(size_t)st * 4]);
+    if (e != cudaSuccess) rc = cuda_fail(e, "step kernels");
+    src = T_out;
+  }
+  if (rc == HS2G_OK) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = cuda_fail(e, "run");
+  }
+  kernel_ms[0] = kernel_ms[1] = kernel_ms[2] = kernel_ms[3] = 0.0;
+  for (int st = 0; st < nsteps && rc == HS2G_OK; ++st)
+    for (int k = 0; k < 3; ++k) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[(size_t)st * 4 + k], ev[(size_t)st * 4 + k + 1]);
+      kernel_ms[k] += ms;
+    }
+  if (rc == HS2G_OK && nsteps > 0) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev[0], ev[(size_t)(nsteps - 1) * 4 + 3]);
+    kernel_ms[3] = ms;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return rc;
+}
+
+int hs2g_fp64_fma_rate(int device, double* fma_per_s) {
+  if (!fma_per_s) return fail(HS2G_ERR_ARG, "null argument");
+  DeviceGuard g(device);
+  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", device);
+  cudaError_t e = hs2g::fp64_fma_rate(fma_per_s);
+  if (e != cudaSuccess) return cuda_fail(e, "fp64 probe");
+  return HS2G_OK;
+}
+
+int hs2g_get_faces(hs2g_handle* h, double* Gz, double* Gy, double* Gx, double* capacity, uint8_t* fixed) {
+  if (!h) return fail(HS2G_ERR_ARG, "null handle");
+  DeviceGuard g(h->device);
+  const Dims& d = h->d;
+  const int64_t n = d.nvox();
+  cudaStream_t s = h->stream;
+  if (Gz) HS2G_CUDA(cudaMemcpyAsync(Gz, h->Gz, sizeof(double) * (d.nz + 1) * d.nxy(), cudaMemcpyDeviceToHost, s), "Gz");
+  if (Gy)
+    HS2G_CUDA(cudaMemcpyAsync(Gy, h->Gy, sizeof(double) * d.nz * (d.ny + 1) * d.nx, cudaMemcpyDeviceToHost, s), "Gy");
+  if (Gx)
+    HS2G_CUDA(cudaMemcpyAsync(Gx, h->Gx, sizeof(double) * d.nz * d.ny * (d.nx + 1), cudaMemcpyDeviceToHost, s), "Gx");
+  if (capacity) HS2G_CUDA(cudaMemcpyAsync(capacity, h->M, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "M");
+  std::vector<uint8_t> comp;
+  if (fixed) {
+    comp.resize((size_t)n);
+    HS2G_CUDA(cudaMemcpyAsync(comp.data(), h->compute, (size_t)n, cudaMemcpyDeviceToHost, s), "mask");
+  }
+  HS2G_CUDA(cudaStreamSynchronize(s), "get faces");
+  if (fixed)
+    for (int64_t v = 0; v < n; ++v) fixed[v] = comp[(size_t)v] ? 0 : 1;
+  return HS2G_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,81 @@
+// Internal declarations shared by the hs2g translation units (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/hs2g.h"
+
+namespace hs2g {
+
+// Grid dimensions; voxel p = (k*ny + j)*nx + i.
+struct Dims {
+  int64_t nz, ny, nx;
+  __host__ __device__ int64_t nvox() const { return nz * ny * nx; }
+  __host__ __device__ int64_t nxy() const { return ny * nx; }
+};
+
+// Per-voxel coefficients of the scaled delta-form Douglas step, structure of arrays in voxel order.
+//   stage 0 (x lines):  z_i = wc*T + wxl*T[i-1] + wxh*T[i+1] + wyl*T[j-1] + wyh*T[j+1] + wzl*T[k-1]
+//                             + wzh*T[k+1] + wq*Q - a0*z_{i-1};   W0_i = z_i - b0*W0_{i+1}
+//   stage 1 (y lines):  z_j = W0_j - a1*z_{j-1};                   W1_j = z_j - b1*W1_{j+1}
+//   stage 2 (z lines):  z_k = W1_k - a2*z_{k-1};                   dT_k = z_k - b2*dT_{k+1};  T' = T + dT
+struct Coeffs {
+  double* wc;
+  double* wxl;
+  double* wxh;
+  double* wyl;
+  double* wyh;
+  double* wzl;
+  double* wzh;
+  double* wq;
+  double* a0;
+  double* b0;
+  double* a1;
+  double* b1;
+  double* a2;
+  double* b2;
+};
+constexpr int kNumCoeffArrays = 14;
+
+struct QTable {
+  double q[HS2G_MAX_CLASSES];
+};
+
+// First error recorded by a device kernel: (code << 56) | (axis << 54) | index, 0 when none.
+__device__ __forceinline__ void record_error(unsigned long long* err, int code, int axis, int64_t index) {
+  unsigned long long v = ((unsigned long long)(-code) << 56) | ((unsigned long long)axis << 54) |
+                         ((unsigned long long)index & ((1ull << 54) - 1));
+  atomicCAS(err, 0ull, v);
+}
+
+// setup kernels (hs2g_compile.cu)
+cudaError_t launch_faces(const Dims& d, int axis, const uint8_t* material, const uint8_t* bclass,
+                         const hs2g_material* mats, int nmat, const hs2g_face_form* forms, int nbnd, double* G,
+                         unsigned long long* err, cudaStream_t s);
+cudaError_t launch_capacity_from_classes(const Dims& d, const uint8_t* material, const hs2g_material* mats,
+                                         int nmat, double* M, uint8_t* compute, unsigned long long* err,
+                                         cudaStream_t s);
+cudaError_t launch_validate_dense(const Dims& d, const double* Gz, const double* Gy, const double* Gx,
+                                  double* M, uint8_t* compute, unsigned long long* err, cudaStream_t s);
+cudaError_t launch_factor(const Dims& d, const double* Gz, const double* Gy, const double* Gx, const double* M,
+                          const uint8_t* compute, double* s2, double* sigma, const Coeffs& c, cudaStream_t s);
+
+// step kernels (hs2g_sweep.cu)
+struct StepArgs {
+  Dims d;
+  const double* T_in;
+  double* T_out;
+  double* W0;
+  double* W1;
+  const uint8_t* vclass;
+  const double* qdense;  // may be null
+  bool has_qtab;
+};
+cudaError_t launch_step(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s);
+// the same three kernels with an event recorded before each and after the last (ev[0..3])
+cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s,
+                               cudaEvent_t ev[4]);
+cudaError_t fp64_fma_rate(double* fma_per_s);
+cudaError_t launch_copy_layer(const Dims& d, const double* T, int layer, double* dst, cudaStream_t s);
+
+}  // namespace hs2g

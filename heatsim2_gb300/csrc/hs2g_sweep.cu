@@ -1,0 +1,274 @@
+// The per-step sweep kernels: one Douglas ADI timestep in scaled delta form (see hs2g_compile.cu for the
+// algebra and hs2g_internal.cuh for the coefficient layout).  Replaces, per timestep, the reference's
+// source-field assembly and three permute / CSR mat-vec / tridiagonal-solve stages
+// (alternatingdirection_c_pyx.pyx:294-416, tridiag.pyx:46-69).
+//
+// FP64 is the binding resource on GB300 (about 0.6e12 DFMA/s against ~6.5 TB/s of HBM), so the step is
+// arranged for the fewest FP64 operations: 7 stencil FMAs (+1 when a source is active) and 2 recurrence
+// FMAs per voxel in the x sweep, 2 FMAs per voxel in the y sweep, 2 FMAs and 1 add per voxel in the z sweep.
+//
+// Memory layout: every array is (nz, ny, nx) with x fastest.
+//   x sweep: a CTA owns 32 consecutive x-lines.  The stencil is evaluated in 32-column chunks with lanes
+//            along x (coalesced loads of T and the coefficients), staged through shared memory, and one warp
+//            runs the line recurrences down the transposed chunk (lane = line).  The forward values are kept
+//            in the output array W0 and re-read by the back substitution in the same CTA.
+//   y sweep: one thread per y-line (k,i); neighbouring lanes have neighbouring i, so each j step is one
+//            coalesced 256-byte load per array per warp.
+//   z sweep: one thread per z-line (j,i), same coalescing argument with stride ny*nx.
+#include "hs2g_internal.cuh"
+
+namespace hs2g {
+namespace {
+
+constexpr int kXLines = 32;   // x-lines per CTA
+constexpr int kXChunk = 32;   // columns per staged chunk
+constexpr int kXThreads = 128;
+constexpr int kXWarps = kXThreads / 32;
+constexpr int kXLinesPerWarp = kXLines / kXWarps;
+constexpr int kLineThreads = 128;
+
+template <bool HAS_Q>
+__global__ void __launch_bounds__(kXThreads) sweep_x_kernel(Dims d, const double* __restrict__ T, Coeffs c,
+                                                             const uint8_t* __restrict__ vclass,
+                                                             const double* __restrict__ qdense, QTable qt,
+                                                             double* __restrict__ W0) {
+  __shared__ double sr[kXLines][kXChunk + 1];
+  __shared__ double sa[kXLines][kXChunk + 1];
+  __shared__ double sq[HAS_Q ? HS2G_MAX_CLASSES : 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (HAS_Q) {
+    for (int e = threadIdx.x; e < HS2G_MAX_CLASSES; e += kXThreads) sq[e] = qt.q[e];
+  }
+  const int64_t nlines = d.nz * d.ny;
+  const int64_t L0 = (int64_t)blockIdx.x * kXLines;
+  const int64_t nxy = d.nxy();
+  const int nchunks = (int)((d.nx + kXChunk - 1) / kXChunk);
+  __syncthreads();
+
+  // forward: z_i = R'_i - a0_i * z_{i-1}
+  double carry = 0.0;
+  for (int ch = 0; ch < nchunks; ++ch) {
+    const int64_t i = (int64_t)ch * kXChunk + lane;
+#pragma unroll
+    for (int ll = 0; ll < kXLinesPerWarp; ++ll) {
+      const int l = warp * kXLinesPerWarp + ll;
+      const int64_t L = L0 + l;
+      double r = 0.0, a = 0.0;
+      if (L < nlines && i < d.nx) {
+        const int64_t k = L / d.ny, j = L - k * d.ny;
+        const int64_t p = L * d.nx + i;
+        const double t = T[p];
+        // out-of-grid neighbours carry a zero coefficient (exterior faces are insulating): read T[p] instead
+        const double txl = i > 0 ? T[p - 1] : t;
+        const double txh = i + 1 < d.nx ? T[p + 1] : t;
+        const double tyl = j > 0 ? T[p - d.nx] : t;
+        const double tyh = j + 1 < d.ny ? T[p + d.nx] : t;
+        const double tzl = k > 0 ? T[p - nxy] : t;
+        const double tzh = k + 1 < d.nz ? T[p + nxy] : t;
+        r = c.wc[p] * t;
+        r = fma(c.wxl[p], txl, r);
+        r = fma(c.wxh[p], txh, r);
+        r = fma(c.wyl[p], tyl, r);
+        r = fma(c.wyh[p], tyh, r);
+        r = fma(c.wzl[p], tzl, r);
+        r = fma(c.wzh[p], tzh, r);
+        if (HAS_Q) {
+          double q = sq[vclass[p]];
+          if (qdense) q += qdense[p];
+          r = fma(c.wq[p], q, r);
+        }
+        a = c.a0[p];
+      }
+      sr[l][lane] = r;
+      sa[l][lane] = a;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      const int cw = (int)min((int64_t)kXChunk, d.nx - (int64_t)ch * kXChunk);
+      double z = carry;
+      for (int cc = 0; cc < cw; ++cc) {
+        z = fma(-sa[lane][cc], z, sr[lane][cc]);
+        sr[lane][cc] = z;
+      }
+      carry = z;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ll = 0; ll < kXLinesPerWarp; ++ll) {
+      const int l = warp * kXLinesPerWarp + ll;
+      const int64_t L = L0 + l;
+      if (L < nlines && i < d.nx) W0[L * d.nx + i] = sr[l][lane];
+    }
+    __syncthreads();
+  }
+
+  // back substitution: W0_i = z_i - b0_i * W0_{i+1}
+  carry = 0.0;
+  for (int ch = nchunks - 1; ch >= 0; --ch) {
+    const int64_t i = (int64_t)ch * kXChunk + lane;
+#pragma unroll
+    for (int ll = 0; ll < kXLinesPerWarp; ++ll) {
+      const int l = warp * kXLinesPerWarp + ll;
+      const int64_t L = L0 + l;
+      double z = 0.0, b = 0.0;
+      if (L < nlines && i < d.nx) {
+        const int64_t p = L * d.nx + i;
+        z = W0[p];
+        b = c.b0[p];
+      }
+      sr[l][lane] = z;
+      sa[l][lane] = b;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      const int cw = (int)min((int64_t)kXChunk, d.nx - (int64_t)ch * kXChunk);
+      double x = carry;
+      for (int cc = cw - 1; cc >= 0; --cc) {
+        x = fma(-sa[lane][cc], x, sr[lane][cc]);
+        sr[lane][cc] = x;
+      }
+      carry = x;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ll = 0; ll < kXLinesPerWarp; ++ll) {
+      const int l = warp * kXLinesPerWarp + ll;
+      const int64_t L = L0 + l;
+      if (L < nlines && i < d.nx) W0[L * d.nx + i] = sr[l][lane];
+    }
+    __syncthreads();
+  }
+}
+
+// y lines: W1 = s2 * dT1 from W0 = sigma * dT0
+__global__ void __launch_bounds__(kLineThreads) sweep_y_kernel(Dims d, const double* __restrict__ W0,
+                                                                const double* __restrict__ a1,
+                                                                const double* __restrict__ b1,
+                                                                double* __restrict__ W1) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= d.nz * d.nx) return;
+  const int64_t k = t / d.nx, i = t - k * d.nx;
+  int64_t p = k * d.nxy() + i;
+  double z = 0.0;
+#pragma unroll 4
+  for (int64_t j = 0; j < d.ny; ++j, p += d.nx) {
+    z = fma(-a1[p], z, W0[p]);
+    W1[p] = z;
+  }
+  double x = 0.0;
+#pragma unroll 4
+  for (int64_t j = d.ny - 1; j >= 0; --j) {
+    p -= d.nx;
+    x = fma(-b1[p], x, W1[p]);
+    W1[p] = x;
+  }
+}
+
+// z lines: dT2 from W1 = s2 * dT1; T_out = T_in + dT2.  Z is scratch (the x sweep's buffer, free by now).
+// T_in may equal T_out: each voxel's T_in is read by the same thread just before its T_out is written.
+__global__ void __launch_bounds__(kLineThreads) sweep_z_kernel(Dims d, const double* __restrict__ W1,
+                                                                const double* __restrict__ a2,
+                                                                const double* __restrict__ b2, const double* T_in,
+                                                                double* __restrict__ Z, double* T_out) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nxy = d.nxy();
+  if (t >= nxy) return;
+  int64_t p = t;
+  double z = 0.0;
+#pragma unroll 4
+  for (int64_t k = 0; k < d.nz; ++k, p += nxy) {
+    z = fma(-a2[p], z, W1[p]);
+    Z[p] = z;
+  }
+  double x = 0.0;
+#pragma unroll 4
+  for (int64_t k = d.nz - 1; k >= 0; --k) {
+    p -= nxy;
+    x = fma(-b2[p], x, Z[p]);
+    T_out[p] = T_in[p] + x;
+  }
+}
+
+__global__ void copy_layer_kernel(Dims d, const double* __restrict__ T, int layer, double* __restrict__ dst) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t < d.nxy()) dst[t] = T[(int64_t)layer * d.nxy() + t];
+}
+
+inline unsigned blocks(int64_t n, int per) { return (unsigned)((n + per - 1) / per); }
+
+// FP64 issue-rate probe: 8 independent FMA chains per thread, registers only, one store per thread.
+__global__ void fp64_probe_kernel(double* out, int iters, double a, double b) {
+  double acc[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc[k] = (double)(threadIdx.x + k);
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc[k] = fma(acc[k], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += acc[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace
+
+cudaError_t fp64_fma_rate(double* fma_per_s) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const int blocksN = sms * 4, threads = 256, iters = 4096;
+  double* out = nullptr;
+  e = cudaMalloc(&out, sizeof(double) * blocksN * threads);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 5; ++rep) {
+    cudaEventRecord(e0, 0);
+    fp64_probe_kernel<<<blocksN, threads>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(e1, 0);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && ms < best) best = ms;
+  }
+  e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  *fma_per_s = (double)blocksN * threads * iters * 8 / (best * 1e-3);
+  return e;
+}
+
+cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s,
+                               cudaEvent_t ev[4]) {
+  const Dims& d = a.d;
+  const bool has_q = a.has_qtab || a.qdense != nullptr;
+  const unsigned gx = blocks(d.nz * d.ny, kXLines);
+  if (ev) cudaEventRecord(ev[0], s);
+  if (has_q)
+    sweep_x_kernel<true><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0);
+  else
+    sweep_x_kernel<false><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0);
+  if (ev) cudaEventRecord(ev[1], s);
+  sweep_y_kernel<<<blocks(d.nz * d.nx, kLineThreads), kLineThreads, 0, s>>>(d, a.W0, c.a1, c.b1, a.W1);
+  if (ev) cudaEventRecord(ev[2], s);
+  sweep_z_kernel<<<blocks(d.nxy(), kLineThreads), kLineThreads, 0, s>>>(d, a.W1, c.a2, c.b2, a.T_in, a.W0,
+                                                                         a.T_out);
+  if (ev) cudaEventRecord(ev[3], s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s) {
+  return launch_step_events(a, c, q, s, nullptr);
+}
+
+cudaError_t launch_copy_layer(const Dims& d, const double* T, int layer, double* dst, cudaStream_t s) {
+  copy_layer_kernel<<<blocks(d.nxy(), 256), 256, 0, s>>>(d, T, layer, dst);
+  return cudaGetLastError();
+}
+
+}  // namespace hs2g

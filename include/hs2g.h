@@ -1,0 +1,177 @@
+/*
+ * hs2g -- GB300-native ADI Crank-Nicolson heat-conduction timestep (heatsim2's hot path), C ABI.
+ *
+ * This is the native boundary that replaces the reference's Cython extension modules
+ * (heatsim2/alternatingdirection_c_pyx.pyx, heatsim2/crank_nicolson.pyx, heatsim2/tridiag.pyx) and its
+ * hand-written C assembler (heatsim2/alternatingdirection_c.h:50-54).  Plain pointers and sizes only; the
+ * library owns every device allocation it makes, the caller owns every buffer it passes in.
+ *
+ * Conventions
+ *   - every entry point returns HS2G_OK (0) or a negative HS2G_ERR_* code and never exits or aborts
+ *     (the reference's add_equation calls exit(1) on an out-of-domain stencil, alternatingdirection_c.c:160-163);
+ *     hs2g_last_error() describes the last failure of the calling thread;
+ *   - arrays are C-contiguous, z slowest and x fastest: T[k][j][i] with shape (nz, ny, nx), z faces
+ *     (nz+1, ny, nx), y faces (nz, ny+1, nx), x faces (nz, ny, nx+1) (heatsim2/__init__.py:191-197);
+ *   - a handle is used by one host thread at a time; distinct handles may be used concurrently;
+ *   - work is queued on the handle's stream (hs2g_set_stream); HS2G_SYNC waits for it before returning.
+ */
+#ifndef HS2G_H
+#define HS2G_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HS2G_ABI_VERSION 1
+
+#define HS2G_OK 0
+#define HS2G_ERR_ARG (-1)        /* bad argument (shape, pointer, class index out of range) */
+#define HS2G_ERR_CUDA (-2)       /* a CUDA runtime call failed */
+#define HS2G_ERR_NOMEM (-3)      /* device or pinned-host allocation failed */
+#define HS2G_ERR_EXTERIOR (-4)   /* a compute voxel has a non-insulating face on the grid's exterior */
+#define HS2G_ERR_KTYPE (-5)      /* a boundary class needs scalar k but the material has a matrix, or reverse */
+#define HS2G_ERR_UNALIGNED (-6)  /* a face flux couples across axes (anisotropy not aligned with the grid) */
+#define HS2G_ERR_FORM (-7)       /* a face flux is not a conservative Crank-Nicolson two-point difference */
+#define HS2G_ERR_CAPACITY (-8)   /* a computed voxel has rho*c/dt <= 0 or not finite */
+#define HS2G_ERR_STATE (-9)      /* handle not in a state that allows this call */
+
+/* flags */
+#define HS2G_DEVICE 1            /* T_in / T_out / qdense / history are device pointers (no copies) */
+#define HS2G_SYNC 2              /* synchronise the handle's stream before returning */
+
+/* material kinds (heatsim2/__init__.py:42-43) */
+#define HS2G_TEMPERATURE_COMPUTE 0
+#define HS2G_TEMPERATURE_FIXED 1
+
+/* source kinds evaluated per class by hs2g_source_table (heatsim2/__init__.py:46-50) */
+#define HS2G_NO_SOURCE 0
+#define HS2G_IMPULSE_SOURCE 1
+#define HS2G_STEPPED_SOURCE 2
+#define HS2G_IMPULSE_POINT_SOURCE_JOULES 3
+
+/*
+ * A face flux coefficient as an affine form in the conductivity entries of the two materials that meet at the
+ * face (after the reference's neighbour-k fallback, crank_nicolson.pyx:298-338):
+ *     value = f[0] + sum_e f[1+e] * k_lo[e] + sum_e f[1+HS2G_K_ENTRIES+e] * k_hi[e]
+ * k entry 0 is a scalar conductivity, entries 1..9 the 3x3 tensor (row-major, z,y,x order).  A material holds
+ * NaN in the representation it does not have; a form with a non-zero coefficient on such an entry raises
+ * HS2G_ERR_KTYPE for the faces that use it.
+ */
+#define HS2G_K_ENTRIES 10
+#define HS2G_FORM_LEN (1 + 2 * HS2G_K_ENTRIES)
+#define HS2G_MAX_ZERO_FORMS 24
+#define HS2G_MAX_CLASSES 256
+
+typedef struct {
+  int32_t kind;                     /* HS2G_TEMPERATURE_COMPUTE / _FIXED */
+  double k[HS2G_K_ENTRIES];         /* scalar k in k[0] or tensor in k[1..9]; NaN where absent */
+  double capacity;                  /* rho * c * (1/dt) in W/m^3/K (crank_nicolson.pyx:378) */
+} hs2g_material;
+
+/*
+ * A boundary class evaluated on one axis (0 = z, 1 = y, 2 = x): the heat-balance conductance of the face,
+ * G (W/m^3/K) = normal . [1, k_lo, k_hi], i.e. the flux divided by the cell size is -G * (T_hi - T_lo)
+ * (crank_nicolson.pyx:359-363).  zero[z] are forms that must vanish on every face that uses the class
+ * (cross-axis terms, unbalanced two-point terms, terms outside a Crank-Nicolson group, constant fluxes);
+ * zero_code[z] is the HS2G_ERR_* raised when one does not.
+ */
+typedef struct {
+  double normal[HS2G_FORM_LEN];
+  int32_t nzero;
+  int32_t zero_code[HS2G_MAX_ZERO_FORMS];
+  double zero[HS2G_MAX_ZERO_FORMS][HS2G_FORM_LEN];
+} hs2g_face_form;
+
+/* Problem described by class arrays: what heatsim2.setup receives (crank_nicolson.pyx:128-142). */
+typedef struct {
+  int64_t nz, ny, nx;
+  int32_t nmat, nbnd;
+  const hs2g_material* materials;   /* [nmat] */
+  const hs2g_face_form* forms;      /* [nbnd][3] */
+  const uint8_t* material;          /* (nz, ny, nx) */
+  const uint8_t* boundary_z;        /* (nz+1, ny, nx) */
+  const uint8_t* boundary_y;        /* (nz, ny+1, nx) */
+  const uint8_t* boundary_x;        /* (nz, ny, nx+1) */
+  const uint8_t* volumetric;        /* (nz, ny, nx) source class of each voxel */
+} hs2g_class_problem;
+
+/* Problem described by per-face conductances and per-voxel capacities (continuous, per-voxel k / rho*c).
+   Faces of fixed voxels are ignored; exterior faces of computed voxels must be zero. */
+typedef struct {
+  int64_t nz, ny, nx;
+  const double* Gz;                 /* (nz+1, ny, nx) W/m^3/K */
+  const double* Gy;                 /* (nz, ny+1, nx) */
+  const double* Gx;                 /* (nz, ny, nx+1) */
+  const double* capacity;           /* (nz, ny, nx) rho*c/dt, W/m^3/K */
+  const uint8_t* fixed;             /* (nz, ny, nx) 1 = fixed temperature, or NULL for none */
+  const uint8_t* volumetric;        /* (nz, ny, nx) source classes, or NULL for class 0 everywhere */
+} hs2g_dense_problem;
+
+typedef struct hs2g_handle hs2g_handle;
+
+int hs2g_abi_version(void);
+const char* hs2g_last_error(void);
+
+/* Compile a problem onto device `device` (replaces setup's voxel loop and per-stage assembly + LU:
+   crank_nicolson.pyx:272-496, alternatingdirection_c.c:56-199 create_adi_step/add_equation,
+   alternatingdirection_c_pyx.pyx:212-282 finalize, tridiag.pyx:9-43 tridiaglu). */
+int hs2g_create_classes(const hs2g_class_problem* problem, int device, hs2g_handle** out);
+int hs2g_create_dense(const hs2g_dense_problem* problem, int device, hs2g_handle** out);
+/* Free every device buffer of the handle (replaces delete_adi_step, alternatingdirection_c.c:14-54). */
+void hs2g_destroy(hs2g_handle* h);
+
+/* Queue subsequent work on `stream` (a cudaStream_t; NULL = the handle's own stream). */
+int hs2g_set_stream(hs2g_handle* h, void* stream);
+int hs2g_shape(const hs2g_handle* h, int64_t shape[3]);
+
+/*
+ * One timestep T_out = ADI(T_in) (replaces run_adi_steps' stage loop, alternatingdirection_c_pyx.pyx:387-416,
+ * and tridiagsolve, tridiag.pyx:46-69).
+ *   qtab      host array of HS2G_MAX_CLASSES source values (W/m^3) per volumetric class for this step,
+ *             or NULL when no class source is active;
+ *   qdense    per-voxel source added to the class sources (W/m^3), or NULL;
+ *   volumetric  replacement (nz,ny,nx) source-class map (host), or NULL to keep the current one.
+ * T_out may equal T_in.  Fixed-temperature voxels keep T_in.
+ */
+int hs2g_step(hs2g_handle* h, const double* T_in, double* T_out, const double* qtab, const double* qdense,
+              const uint8_t* volumetric, int flags);
+
+/*
+ * nsteps timesteps on the device (one CUDA graph per step shape).  qtabs is a host array
+ * [nsteps][HS2G_MAX_CLASSES] of per-step class sources or NULL.  When history is not NULL, the layer
+ * z = record_layer of T after every step is written to history[nsteps][ny][nx].
+ */
+int hs2g_run(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, const double* qtabs,
+             int record_layer, double* history, int flags);
+
+/*
+ * hs2g_run without history, timing each sweep kernel with CUDA events on the handle's stream.
+ * kernel_ms[0..2] receive the summed device time of the x, y and z sweeps over the nsteps steps and
+ * kernel_ms[3] the device time from the first event to the last.  Takes device pointers (HS2G_DEVICE).
+ */
+int hs2g_run_timed(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, const double* qtabs, int flags,
+                   double* kernel_ms);
+
+/* Measured FP64 fused-multiply-add issue rate of `device` (FMA/s): a register-only kernel with 8 independent
+   chains per thread on every SM, timed with CUDA events.  The FP64 roofline denominator for the sweeps. */
+int hs2g_fp64_fma_rate(int device, double* fma_per_s);
+
+/* Per-class source values at time t (alternatingdirection_c_pyx.pyx:294-319 for the class-uniform kinds):
+   kind[c] in HS2G_*_SOURCE, params[c*4 .. c*4+3] = the tuple's numbers after the kind;
+   volume = dz*dy*dx for IMPULSE_POINT_SOURCE_JOULES.  Writes qtab[0..HS2G_MAX_CLASSES-1]; returns the
+   number of classes with a non-zero value (>= 0) or an error. */
+int hs2g_source_table(int nsrc, const int32_t* kind, const double* params, double t, double dt, double volume,
+                      double* qtab);
+
+/* Copy the compiled face conductances and capacities to host buffers (any may be NULL). */
+int hs2g_get_faces(hs2g_handle* h, double* Gz, double* Gy, double* Gx, double* capacity, uint8_t* fixed);
+
+/* Device bytes held by the handle. */
+int64_t hs2g_device_bytes(const hs2g_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

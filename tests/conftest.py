@@ -1,0 +1,52 @@
+import glob
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+for p in (ROOT, os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a) and the built libhs2g.so")
+    config.addinivalue_line("markers", "slow: long-running")
+
+
+def golden_files(include_big=True):
+    out = []
+    for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
+        b = os.path.basename(f)
+        if b.startswith("stages_") or b == "tridiag.npz":
+            continue
+        out.append(f)
+    return out
+
+
+def load_golden(path):
+    from heatsim2_gb300 import workloads as W
+    z = np.load(path)
+    spec = W.spec_from_npz(z)
+    steps = {int(k[2:]): np.array(z[k]) for k in z.files if k.startswith("T_")}
+    return spec, [float(t) for t in z["times"]], steps
+
+
+def rel_err(a, ref):
+    a = np.asarray(a)
+    ref = np.asarray(ref)
+    return float(np.abs(a - ref).max() / np.abs(ref).max())
+
+
+@pytest.fixture(scope="session")
+def cuda_ok():
+    try:
+        import torch
+    except ImportError:
+        pytest.skip("torch missing")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return True

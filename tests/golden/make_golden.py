@@ -1,0 +1,106 @@
+"""Generate the golden fixtures in tests/golden/ by running the reference heatsim2 itself.
+
+Run in a container where the reference sources are mounted (the reference is built into oracle/_ref by
+oracle/build_ref.py first):
+
+    python oracle/build_ref.py && python tests/golden/make_golden.py
+
+Each fixture ``<name>.npz`` holds the problem spec (heatsim2_gb300.workloads serialisation), the t values
+passed to the reference's run_adi_steps, and the temperature field the reference returned after selected
+steps.  ``stages_<name>.npz`` additionally holds the reference's per-stage tridiagonal A, sparse B / C and D
+(alternatingdirection_c_pyx.pyx:120-284) for the coefficient-compiler tests, and ``tridiag.npz`` holds
+tridiaglu / tridiagsolve results (tridiag.pyx:9-69) on random diagonally dominant systems.
+"""
+import contextlib
+import io
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import build_ref  # noqa: E402
+from heatsim2_gb300 import workloads as W  # noqa: E402
+
+
+def quiet(fn, *a, **k):
+    with contextlib.redirect_stdout(io.StringIO()):
+        return fn(*a, **k)
+
+
+def run_reference(hs, spec, save_steps):
+    P, S = quiet(hs.setup, *W.setup_args(hs, spec))
+    vol = W.volumetric_tuple(hs, spec)
+    T = W.initial_temperature(spec)
+    times = W.step_times(spec)
+    out = {}
+    for n, t in enumerate(times):
+        T = hs.run_adi_steps(P, S, t, spec["dt"], T, spec["arrays"]["volumetric"], vol)
+        if (n + 1) in save_steps:
+            out["T_%d" % (n + 1)] = np.array(T)
+    return P, S, times, out
+
+
+def save_fixture(name, spec, save_steps, hs, stages=False):
+    P, S, times, res = run_reference(hs, spec, save_steps)
+    d = W.spec_to_npz_dict(spec)
+    d.update(res)
+    d["times"] = np.array(times)
+    d["save_steps"] = np.array(sorted(save_steps))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+    if stages:
+        sd = {}
+        for s, st in enumerate(S):
+            sd["A_%d" % s] = np.array(st.Amat)
+            sd["D_%d" % s] = np.array(st.Dvec)
+            sd["perm_%d" % s] = np.array(st.permuteorder)
+            B = st.Bmat.tocoo()
+            sd["B_%d_row" % s], sd["B_%d_col" % s], sd["B_%d_val" % s] = B.row, B.col, B.data
+            for c, C in enumerate(st.Cmats):
+                C = C.tocoo()
+                sd["C_%d_%d_row" % (s, c)], sd["C_%d_%d_col" % (s, c)], sd["C_%d_%d_val" % (s, c)] = \
+                    C.row, C.col, C.data
+        np.savez_compressed(os.path.join(HERE, "stages_" + name + ".npz"), **sd)
+    print("wrote", name, sorted(res))
+
+
+def tridiag_fixture(hs_tridiag):
+    rng = np.random.default_rng(11)
+    d = {}
+    for c, n in enumerate((1, 2, 5, 40, 64)):
+        A = rng.uniform(-1, 1, size=(n, 3))
+        A[:, 1] = 2.5 + rng.uniform(0, 1, size=n)
+        A[0, 0] = 0.0
+        A[-1, 2] = 0.0
+        b = rng.uniform(-1, 1, size=n)
+        L, U = hs_tridiag.tridiaglu(A.copy())
+        x = hs_tridiag.tridiagsolve(L, U, b.copy())
+        d["A_%d" % c], d["b_%d" % c], d["L_%d" % c], d["U_%d" % c], d["x_%d" % c] = A, b, L, U, x
+    np.savez_compressed(os.path.join(HERE, "tridiag.npz"), **d)
+    print("wrote tridiag")
+
+
+def main():
+    if not build_ref.available():
+        build_ref.build()
+    hs = build_ref.import_reference()
+    import heatsim2.tridiag as ref_tridiag
+    tridiag_fixture(ref_tridiag)
+
+    save_fixture("steel_slab", W.steel_slab(), {1, 2, 10, 50, 200}, hs)
+    save_fixture("composite_small",
+                 W.composite_panel(seed=1, nz=24, ny=32, nx=32, top_layers=6, width_range=(4, 12),
+                                   depth_range=(2, 12), nsteps=20),
+                 {1, 5, 20}, hs, stages=False)
+    save_fixture("mixed_small", W.mixed_small(), set(range(1, 7)), hs, stages=True)
+    save_fixture("sources_small", W.sources_small(), set(range(1, 6)), hs, stages=True)
+    for shape in ((1, 1, 7), (7, 1, 1), (1, 7, 1), (1, 1, 1), (1, 5, 6), (4, 1, 5), (3, 4, 1)):
+        save_fixture("line_%dx%dx%d" % shape, W.line_grid(shape), set(range(1, 6)), hs)
+
+
+if __name__ == "__main__":
+    main()

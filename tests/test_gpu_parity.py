@@ -1,0 +1,273 @@
+"""GPU parity: the CUDA path (libhs2g through heatsim2_gb300.setup / run_adi_steps) against the reference's
+golden outputs and the oracle.  Bar: max|T_gpu - T_ref| / max|T_ref| <= 1e-12 (FP64, the tolerance the
+reference comparison is specified at)."""
+import numpy as np
+import pytest
+
+from conftest import golden_files, load_golden, rel_err, GOLDEN
+import oracle
+from oracle_shim import HS
+import heatsim2_gb300 as hs
+from heatsim2_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def _setup(spec):
+    return hs.setup(*W.setup_args(hs, spec))
+
+
+def _run_host(spec, times, P, S, T=None):
+    vol = W.volumetric_tuple(hs, spec)
+    T = W.initial_temperature(spec) if T is None else T
+    out = {}
+    for n, t in enumerate(times):
+        T = hs.run_adi_steps(P, S, t, spec["dt"], T, spec["arrays"]["volumetric"], vol)
+        out[n + 1] = T
+    return out
+
+
+@pytest.mark.parametrize("path", golden_files(), ids=lambda p: p.rsplit("/", 1)[-1])
+def test_golden_parity(cuda_ok, path):
+    spec, times, ref = load_golden(path)
+    P, S = _setup(spec)
+    got = _run_host(spec, times, P, S)
+    for n, T in ref.items():
+        assert rel_err(got[n], T) <= TOL, (n, rel_err(got[n], T))
+
+
+def test_device_tensor_path_equals_host_path(cuda_ok):
+    import torch
+    spec, times, ref = load_golden(GOLDEN + "/steel_slab.npz")
+    P, S = _setup(spec)
+    vol = W.volumetric_tuple(hs, spec)
+    T = torch.from_numpy(W.initial_temperature(spec)).cuda()
+    host = _run_host(spec, times[:50], P, S)
+    for n, t in enumerate(times[:50]):
+        T = hs.run_adi_steps(P, S, t, spec["dt"], T, spec["arrays"]["volumetric"], vol)
+    np.testing.assert_array_equal(T.cpu().numpy(), host[50])
+    assert rel_err(T.cpu().numpy(), ref[50]) <= TOL
+
+
+def test_run_equals_single_steps_and_records_history(cuda_ok):
+    spec, times, ref = load_golden(GOLDEN + "/sources_small.npz")
+    P, S = _setup(spec)
+    vol = W.volumetric_tuple(hs, spec)
+    host = _run_host(spec, times, P, S)
+    T, hist = hs.run(P, W.initial_temperature(spec), times, spec["dt"], spec["arrays"]["volumetric"], vol,
+                     record_layer=0)
+    np.testing.assert_array_equal(T, host[len(times)])
+    for n in range(len(times)):
+        np.testing.assert_array_equal(hist[n], host[n + 1][0])
+
+
+def test_run_device_many_steps(cuda_ok):
+    import torch
+    spec, times, ref = load_golden(GOLDEN + "/steel_slab.npz")
+    P, S = _setup(spec)
+    vol = W.volumetric_tuple(hs, spec)
+    T0 = torch.from_numpy(W.initial_temperature(spec)).cuda()
+    T, hist = hs.run(P, T0, times, spec["dt"], spec["arrays"]["volumetric"], vol, record_layer=0)
+    assert rel_err(T.cpu().numpy(), ref[200]) <= TOL
+    assert rel_err(hist[9].cpu().numpy(), ref[10][0]) <= TOL
+    assert torch.equal(T0, torch.from_numpy(W.initial_temperature(spec)).cuda())   # input untouched
+
+
+def _coo_dense(z, prefix, n):
+    M = np.zeros((n, n))
+    np.add.at(M, (z[prefix + "_row"], z[prefix + "_col"]), z[prefix + "_val"])
+    return M
+
+
+@pytest.mark.parametrize("name", ["mixed_small", "sources_small"])
+def test_compiled_stage_matrices_match_reference(cuda_ok, name):
+    """The device coefficient compiler produces the reference's stage matrices (pyadi_step.Amat/Bmat/Cmats/Dvec)."""
+    spec, _, _ = load_golden(GOLDEN + "/%s.npz" % name)
+    st = np.load(GOLDEN + "/stages_%s.npz" % name)
+    P, S = _setup(spec)
+    n = W.voxels(spec)
+    for s in range(3):
+        np.testing.assert_allclose(S[s].Amat, st["A_%d" % s], rtol=1e-14, atol=0)
+        np.testing.assert_array_equal(S[s].Dvec, st["D_%d" % s])
+        np.testing.assert_allclose(S[s].Bmat.toarray(), _coo_dense(st, "B_%d" % s, n), rtol=1e-13, atol=1e-6)
+        for c in range(s):
+            np.testing.assert_allclose(S[s].Cmats[c].toarray(), _coo_dense(st, "C_%d_%d" % (s, c), n),
+                                       rtol=1e-13, atol=1e-6)
+        assert S[s].permuteorder == tuple(st["perm_%d" % s])
+
+
+def _compare_with_oracle(spec, nsteps, tol=TOL):
+    P, S = _setup(spec)
+    Po, _ = oracle.setup(*W.setup_args(HS, spec))
+    vol = W.volumetric_tuple(hs, spec)
+    volo = W.volumetric_tuple(HS, spec)
+    T = W.initial_temperature(spec)
+    To = T.copy()
+    worst = 0.0
+    for n, t in enumerate(W.step_times(spec, nsteps)):
+        T = hs.run_adi_steps(P, S, t, spec["dt"], T, spec["arrays"]["volumetric"], vol)
+        To = oracle.run_adi_steps(Po, None, t, spec["dt"], To, spec["arrays"]["volumetric"], volo)
+        worst = max(worst, rel_err(T, To))
+    assert worst <= tol, worst
+    return T
+
+
+def test_composite_panel_midsize_vs_oracle(cuda_ok):
+    spec = W.composite_panel(seed=3, nz=40, ny=96, nx=80, top_layers=10, width_range=(8, 30),
+                             depth_range=(3, 30))
+    _compare_with_oracle(spec, 25)
+
+
+def test_uneven_instances_vs_oracle(cuda_ok):
+    for spec in W.uneven_batch(seed=2, n=3, nz_range=(16, 24), nxy_range=(40, 70)):
+        _compare_with_oracle(spec, 6)
+
+
+def test_full_size_composite_panel_first_steps_vs_oracle(cuda_ok):
+    """The benchmark workload itself (65x512x512 with the ambient layer), two steps against the oracle."""
+    spec = W.composite_panel(seed=1)
+    _compare_with_oracle(spec, 2)
+
+
+def test_full_size_energy_conservation(cuda_ok):
+    """Insulated composite panel at full size: with every exterior face insulating and no fixed voxels the
+    Douglas step conserves energy exactly in real arithmetic (the conductance operator has zero column sums),
+    so sum(rho*c*dT)*V equals the injected source energy to rounding."""
+    import torch
+    spec = W.composite_panel(seed=1)
+    a = spec["arrays"]
+    a["material"][0] = 0                        # ambient layer becomes composite
+    a["boundary_z"][1] = 0                      # joined by the conducting class
+    P, S = _setup(spec)
+    vol = W.volumetric_tuple(hs, spec)
+    T0 = torch.from_numpy(W.initial_temperature(spec)).cuda()
+    times = W.step_times(spec, 12)
+    T = hs.run(P, T0, times, spec["dt"], a["volumetric"], vol)
+    rc = np.where(a["material"] == 0, 1550.0 * 1100.0, 2700.0 * 900.0)
+    dV = spec["grid"]["dz"] * spec["grid"]["dy"] * spec["grid"]["dx"]
+    energy = float(((T - T0).cpu().numpy() * rc).sum() * dV)
+    injected = 2e9 * spec["dt"] * dV * float((a["volumetric"] == 1).sum())
+    assert abs(energy - injected) <= 1e-9 * injected, (energy, injected)
+
+
+def test_uniform_state_is_steady(cuda_ok):
+    spec = W.composite_panel(seed=1, nz=16, ny=64, nx=64, top_layers=4, width_range=(4, 20), depth_range=(2, 12))
+    spec["volumetric"] = [["none"], ["none"]]
+    P, S = _setup(spec)
+    T = W.initial_temperature(spec)
+    for t in W.step_times(spec, 5):
+        T = hs.run_adi_steps(P, S, t, spec["dt"], T, spec["arrays"]["volumetric"], W.volumetric_tuple(hs, spec))
+    assert np.abs(T - 293.0).max() <= 1e-12 * 293.0
+
+
+def test_in_place_device_step(cuda_ok):
+    import torch
+    from heatsim2_gb300 import _native
+    spec, times, ref = load_golden(GOLDEN + "/mixed_small.npz")
+    P, S = _setup(spec)
+    T = torch.from_numpy(W.initial_temperature(spec)).cuda()
+    L = _native.load()
+    from heatsim2_gb300.alternatingdirection import _ClassSources, source_table
+    src = _ClassSources(W.volumetric_tuple(hs, spec))
+    for t in times:
+        q, _ = source_table(src, t, spec["dt"], P.volume_array)
+        _native.check(L.hs2g_set_stream(P.handle.ptr, torch.cuda.current_stream().cuda_stream))
+        _native.check(L.hs2g_step(P.handle.ptr, T.data_ptr(), T.data_ptr(), q.ctypes.data, None, None,
+                                  _native.DEVICE | _native.SYNC))
+    assert rel_err(T.cpu().numpy(), ref[len(times)]) <= TOL
+
+
+def test_replaced_source_class_map(cuda_ok):
+    spec = W.steel_slab(seed=4, nz=8, ny=12, nx=10, flaw=4, depth_range=(2, 5))
+    P, S = _setup(spec)
+    Po, _ = oracle.setup(*W.setup_args(HS, spec))
+    other = np.zeros_like(spec["arrays"]["volumetric"])
+    other[:, 3:6, 2:7] = 1
+    vol, volo = W.volumetric_tuple(hs, spec), W.volumetric_tuple(HS, spec)
+    T = To = W.initial_temperature(spec)
+    for t in W.step_times(spec, 3):
+        T = hs.run_adi_steps(P, S, t, spec["dt"], T, other, vol)
+        To = oracle.run_adi_steps(Po, None, t, spec["dt"], To, other, volo)
+    assert rel_err(T, To) <= TOL
+
+
+def test_dense_source_on_device(cuda_ok):
+    import torch
+    spec, times, ref = load_golden(GOLDEN + "/sources_small.npz")
+    P, S = _setup(spec)
+    vol = W.volumetric_tuple(hs, spec)
+    T = torch.from_numpy(W.initial_temperature(spec)).cuda()
+    for t in times:
+        T = hs.run_adi_steps(P, S, t, spec["dt"], T, spec["arrays"]["volumetric"], vol)
+    assert rel_err(T.cpu().numpy(), ref[len(times)]) <= TOL
+
+
+# ---- errors where the reference errors (or silently computes outside the domain) ----------------------
+def _expect_setup_error(spec, exc):
+    with pytest.raises(exc):
+        _setup(spec)
+
+
+def test_conducting_exterior_face_is_rejected(cuda_ok):
+    for key, sl in (("boundary_x", (slice(None), slice(None), -1)), ("boundary_y", (slice(None), 0)),
+                    ("boundary_z", (0,))):
+        spec = W.line_grid((3, 4, 5))
+        spec["arrays"][key][sl] = 0
+        _expect_setup_error(spec, ValueError)
+
+
+def test_scalar_class_on_matrix_k_is_rejected(cuda_ok):
+    spec = W.line_grid((3, 4, 5))
+    spec["materials"][0][1] = W.COMPOSITE_K
+    _expect_setup_error(spec, ValueError)
+
+
+def test_unaligned_anisotropy_is_rejected(cuda_ok):
+    spec = W.line_grid((3, 4, 5))
+    spec["materials"][0][1] = [[5.0, 0.3, 0.0], [0.3, 5.0, 0.0], [0.0, 0.0, 5.0]]
+    spec["boundaries"][0] = ["conducting_anisotropic"]
+    with pytest.raises(AssertionError):
+        _setup(spec)
+
+
+def test_zero_capacity_is_rejected(cuda_ok):
+    spec = W.line_grid((3, 4, 5))
+    spec["materials"][0][2] = 0.0
+    _expect_setup_error(spec, ValueError)
+
+
+def test_fixed_voxels_hold_their_temperature(cuda_ok):
+    spec, times, ref = load_golden(GOLDEN + "/mixed_small.npz")
+    P, S = _setup(spec)
+    got = _run_host(spec, times, P, S)
+    fixed = spec["arrays"]["material"] == 3
+    assert fixed.any()
+    np.testing.assert_array_equal(got[len(times)][fixed], 293.0)
+
+
+def test_install_as_heatsim2_runs_user_boundary_module(cuda_ok):
+    import sys
+    import types
+    hs.install_as_heatsim2()
+    try:
+        from heatsim2.expression import group   # the name user boundary classes import
+        m = types.ModuleType("user_thin")
+
+        def q(kl, kh, dz, dy, dx, Tl, Th, *rest):
+            return -1000.0 * group(Th - Tl)
+        m.qz = m.qy = m.qx = q
+        spec = W.steel_slab(seed=0, nz=6, ny=8, nx=8, flaw=3, depth_range=(2, 3))
+        args = list(W.setup_args(hs, spec))
+        args[11] = (args[11][0], args[11][1], (m,))      # user module in place of the thin-layer class
+        P, S = sys.modules["heatsim2"].setup(*args)
+        Po, _ = oracle.setup(*W.setup_args(HS, spec))
+        T = To = W.initial_temperature(spec)
+        vol, volo = W.volumetric_tuple(hs, spec), W.volumetric_tuple(HS, spec)
+        for t in W.step_times(spec, 4):
+            T = hs.run_adi_steps(P, S, t, spec["dt"], T, spec["arrays"]["volumetric"], vol)
+            To = oracle.run_adi_steps(Po, None, t, spec["dt"], To, spec["arrays"]["volumetric"], volo)
+        assert rel_err(T, To) <= TOL
+    finally:
+        for k in [k for k in sys.modules if k == "heatsim2" or k.startswith("heatsim2.")]:
+            del sys.modules[k]
