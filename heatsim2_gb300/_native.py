@@ -16,6 +16,7 @@ ABI_VERSION = 1
 OK = 0
 ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_EXTERIOR, ERR_KTYPE, ERR_UNALIGNED, ERR_FORM, ERR_CAPACITY, ERR_STATE = \
     -1, -2, -3, -4, -5, -6, -7, -8, -9
+ERR_TIMEOUT = -10
 DEVICE, SYNC = 1, 2
 K_ENTRIES = 10
 FORM_LEN = 1 + 2 * K_ENTRIES

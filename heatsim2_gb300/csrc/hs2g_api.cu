@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -25,6 +26,7 @@ struct hs2g_handle {
   uint8_t* compute = nullptr;
   uint8_t* vclass = nullptr;
   double* coef_block = nullptr;
+  int64_t xb_len = 0;
   Coeffs c{};
   // per-step scratch (device)
   double* W0 = nullptr;
@@ -36,6 +38,9 @@ struct hs2g_handle {
   double* hist_dev = nullptr;
   int64_t hist_len = 0;
   unsigned long long* err_dev = nullptr;
+  int* status_dev = nullptr;
+  bool bulk_y = false, bulk_z = false;
+  hs2g::TensorMapCache* tmaps = nullptr;
   int64_t bytes = 0;
 };
 
@@ -156,13 +161,50 @@ int alloc_common(hs2g_handle* h) {
   if ((rc = dalloc(h, &h->W0, n, "stage buffer 0"))) return rc;
   if ((rc = dalloc(h, &h->W1, n, "stage buffer 1"))) return rc;
   if ((rc = dalloc(h, &h->coef_block, n * hs2g::kNumCoeffArrays, "step coefficients"))) return rc;
+  h->c.nchunks = (h->d.nx + 31) / 32;
+  h->xb_len = h->d.nz * h->d.ny * h->c.nchunks * hs2g::kXBlockCoeffs * 32;
+  if ((rc = dalloc(h, &h->c.xb, h->xb_len, "x stencil coefficients"))) return rc;
+  HS2G_CUDA(cudaMemsetAsync(h->c.xb, 0, sizeof(double) * h->xb_len, h->stream), "clear x coefficients");
   if ((rc = dalloc(h, &h->err_dev, 1, "error word"))) return rc;
-  double** slots[hs2g::kNumCoeffArrays] = {&h->c.wc, &h->c.wxl, &h->c.wxh, &h->c.wyl, &h->c.wyh,
-                                           &h->c.wzl, &h->c.wzh, &h->c.wq, &h->c.a0, &h->c.b0,
-                                           &h->c.a1, &h->c.b1, &h->c.a2, &h->c.b2};
+  if ((rc = dalloc(h, &h->status_dev, 1, "status word"))) return rc;
+  double** slots[hs2g::kNumCoeffArrays] = {&h->c.a0, &h->c.b0, &h->c.a1, &h->c.b1, &h->c.a2, &h->c.b2};
   for (int s = 0; s < hs2g::kNumCoeffArrays; ++s) *slots[s] = h->coef_block + (int64_t)s * n;
   HS2G_CUDA(cudaMemsetAsync(h->err_dev, 0, sizeof(unsigned long long), h->stream), "clear error word");
+  HS2G_CUDA(cudaMemsetAsync(h->status_dev, 0, sizeof(int), h->stream), "clear status word");
+  // tensor-tile line sweeps need 16-byte aligned coefficient arrays (an even voxel count) and even row pitches
+  HS2G_CUDA(hs2g::lines_bulk_prepare(), "configure line-sweep kernels");
+  // Kernel variants (defaults are the fastest measured on GB300; the others stay selectable for comparison
+  // and testing): HS2G_LINE_SWEEP=plain the plain-load y sweep, HS2G_Z_SWEEP=tma the TMA tensor-tile z sweep.
+  const char* ymode = getenv("HS2G_LINE_SWEEP");
+  const char* zmode = getenv("HS2G_Z_SWEEP");
+  h->bulk_y = !(ymode && strcmp(ymode, "plain") == 0) && (n % 2 == 0) && hs2g::lines_bulk_supported(h->d, 1);
+  h->bulk_z = (zmode && strcmp(zmode, "tma") == 0) && (n % 2 == 0) && hs2g::lines_bulk_supported(h->d, 2);
+  h->tmaps = hs2g::tensor_map_cache_create();
   return HS2G_OK;
+}
+
+// Step arguments common to every call; T pointers and the source table are filled in by the caller.
+hs2g::StepArgs make_args(const hs2g_handle* h, const double* T_in, const double* T_out) {
+  hs2g::StepArgs a{};
+  a.d = h->d;
+  a.W0 = h->W0;
+  a.W1 = h->W1;
+  a.vclass = h->vclass;
+  a.status = h->status_dev;
+  const bool aligned = ((reinterpret_cast<uintptr_t>(T_in) | reinterpret_cast<uintptr_t>(T_out)) & 15u) == 0;
+  a.bulk_y = h->bulk_y;
+  a.bulk_z = h->bulk_z && aligned;
+  a.tmaps = h->tmaps;
+  return a;
+}
+
+// After a synchronisation: report a bounded device wait that ran out (and clear the word).
+int check_status(hs2g_handle* h) {
+  int v = 0;
+  HS2G_CUDA(cudaMemcpy(&v, h->status_dev, sizeof(int), cudaMemcpyDeviceToHost), "read status word");
+  if (v == 0) return HS2G_OK;
+  cudaMemset(h->status_dev, 0, sizeof(int));
+  return fail(v, "a device wait in a sweep kernel ran out of time (error %d)", v);
 }
 
 int new_handle(int device, const Dims& d, hs2g_handle** out) {
@@ -218,8 +260,12 @@ const char* hs2g_last_error(void) { return g_last_error.c_str(); }
 void hs2g_destroy(hs2g_handle* h) {
   if (!h) return;
   DeviceGuard g(h->device);
-  if (h->stream) cudaStreamSynchronize(h->stream);
+  cudaStreamSynchronize(h->stream);
+  if (h->own_stream) cudaStreamSynchronize(h->own_stream);
   const int64_t n = h->d.nvox();
+  dfree(h, h->status_dev, 1);
+  hs2g::tensor_map_cache_destroy(h->tmaps);
+  h->tmaps = nullptr;
   dfree(h, h->Gz, 0);
   dfree(h, h->Gy, 0);
   dfree(h, h->Gx, 0);
@@ -227,6 +273,7 @@ void hs2g_destroy(hs2g_handle* h) {
   dfree(h, h->compute, n);
   dfree(h, h->vclass, n);
   dfree(h, h->coef_block, 0);
+  dfree(h, h->c.xb, h->xb_len);
   dfree(h, h->W0, n);
   dfree(h, h->W1, n);
   dfree(h, h->Tin_dev, n);
@@ -365,7 +412,7 @@ int hs2g_create_dense(const hs2g_dense_problem* p, int device, hs2g_handle** out
 
 int hs2g_set_stream(hs2g_handle* h, void* stream) {
   if (!h) return fail(HS2G_ERR_ARG, "null handle");
-  h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+  h->stream = (cudaStream_t)stream;
   return HS2G_OK;
 }
 
@@ -419,11 +466,15 @@ int hs2g_step(hs2g_handle* h, const double* T_in, double* T_out, const double* q
   const bool dev = (flags & HS2G_DEVICE) != 0;
   cudaStream_t s = h->stream;
   if (volumetric) HS2G_CUDA(cudaMemcpyAsync(h->vclass, volumetric, (size_t)n, cudaMemcpyHostToDevice, s), "upload classes");
-  hs2g::StepArgs a{};
-  a.d = d;
-  a.W0 = h->W0;
-  a.W1 = h->W1;
-  a.vclass = h->vclass;
+  const double* Tin_d = T_in;
+  double* Tout_d = T_out;
+  if (!dev) {
+    int rc = ensure_staging(h);
+    if (rc) return rc;
+    Tin_d = h->Tin_dev;
+    Tout_d = h->Tout_dev;
+  }
+  hs2g::StepArgs a = make_args(h, Tin_d, Tout_d);
   hs2g::QTable q;
   a.has_qtab = false;
   if (qtab) {
@@ -445,23 +496,19 @@ int hs2g_step(hs2g_handle* h, const double* T_in, double* T_out, const double* q
       a.qdense = h->qdense_dev;
     }
   }
-  if (dev) {
-    a.T_in = T_in;
-    a.T_out = T_out;
-  } else {
-    int rc = ensure_staging(h);
-    if (rc) return rc;
+  if (!dev)
     HS2G_CUDA(cudaMemcpyAsync(h->Tin_dev, T_in, sizeof(double) * n, cudaMemcpyHostToDevice, s), "upload T");
-    a.T_in = h->Tin_dev;
-    a.T_out = h->Tout_dev;
-  }
+  a.T_in = Tin_d;
+  a.T_out = Tout_d;
   cudaError_t e = hs2g::launch_step(a, h->c, q, s);
   if (e != cudaSuccess) return cuda_fail(e, "step kernels");
   if (!dev) {
     HS2G_CUDA(cudaMemcpyAsync(T_out, h->Tout_dev, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "download T");
     HS2G_CUDA(cudaStreamSynchronize(s), "step");
+    return check_status(h);
   } else if (flags & HS2G_SYNC) {
     HS2G_CUDA(cudaStreamSynchronize(s), "step");
+    return check_status(h);
   }
   return HS2G_OK;
 }
@@ -501,11 +548,7 @@ int hs2g_run(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, cons
       hist = h->hist_dev;
     }
   }
-  hs2g::StepArgs a{};
-  a.d = d;
-  a.W0 = h->W0;
-  a.W1 = h->W1;
-  a.vclass = h->vclass;
+  hs2g::StepArgs a = make_args(h, src, dst);
   hs2g::QTable q;
   memset(&q, 0, sizeof(q));
   for (int st = 0; st < nsteps; ++st) {
@@ -536,8 +579,10 @@ int hs2g_run(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, cons
       HS2G_CUDA(cudaMemcpyAsync(history, h->hist_dev, sizeof(double) * nsteps * d.nxy(), cudaMemcpyDeviceToHost, s),
                 "download history");
     HS2G_CUDA(cudaStreamSynchronize(s), "run");
+    return check_status(h);
   } else if (flags & HS2G_SYNC) {
     HS2G_CUDA(cudaStreamSynchronize(s), "run");
+    return check_status(h);
   }
   return HS2G_OK;
 }
@@ -551,11 +596,7 @@ int hs2g_run_timed(hs2g_handle* h, int nsteps, const double* T_in, double* T_out
   cudaStream_t s = h->stream;
   std::vector<cudaEvent_t> ev((size_t)nsteps * 4);
   for (auto& e : ev) HS2G_CUDA(cudaEventCreate(&e), "cudaEventCreate");
-  hs2g::StepArgs a{};
-  a.d = h->d;
-  a.W0 = h->W0;
-  a.W1 = h->W1;
-  a.vclass = h->vclass;
+  hs2g::StepArgs a = make_args(h, T_in, T_out);
   hs2g::QTable q;
   memset(&q, 0, sizeof(q));
   const double* src = T_in;
@@ -577,7 +618,7 @@ int hs2g_run_timed(hs2g_handle* h, int nsteps, const double* T_in, double* T_out
   }
   if (rc == HS2G_OK) {
     cudaError_t e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) rc = cuda_fail(e, "run");
+    rc = (e != cudaSuccess) ? cuda_fail(e, "run") : check_status(h);
   }
   kernel_ms[0] = kernel_ms[1] = kernel_ms[2] = kernel_ms[3] = 0.0;
   for (int st = 0; st < nsteps && rc == HS2G_OK; ++st)

@@ -221,16 +221,19 @@ __global__ void factor_x_kernel(Dims d, const double* __restrict__ Gz, const dou
     const double sg = sigma[p];
     const double f0 = sg / piv;
     const double center = -(((gxl + gxh) + (gyl + gyh)) + (gzl + gzh));
-    c.wc[p] = f0 * center;
-    c.wxl[p] = f0 * gxl;
-    c.wxh[p] = f0 * gxh;
-    c.wyl[p] = f0 * gyl;
-    c.wyh[p] = f0 * gyh;
-    c.wzl[p] = f0 * gzl;
-    c.wzh[p] = f0 * gzh;
-    c.wq[p] = comp ? f0 : 0.0;
-    c.a0[p] = (i > 0) ? sg * r.lo / (piv * sg_prev) : 0.0;
-    c.b0[p] = (i + 1 < d.nx) ? sg * u / sigma[p + 1] : 0.0;
+    double* blk = c.xb + ((t * c.nchunks + i / 32) * kXBlockCoeffs) * 32 + (i % 32);
+    blk[kWc * 32] = f0 * center;
+    blk[kWxl * 32] = f0 * gxl;
+    blk[kWxh * 32] = f0 * gxh;
+    blk[kWyl * 32] = f0 * gyl;
+    blk[kWyh * 32] = f0 * gyh;
+    blk[kWzl * 32] = f0 * gzl;
+    blk[kWzh * 32] = f0 * gzh;
+    blk[kWq * 32] = comp ? f0 : 0.0;
+    const double a0 = (i > 0) ? sg * r.lo / (piv * sg_prev) : 0.0;
+    const double b0 = (i + 1 < d.nx) ? sg * u / sigma[p + 1] : 0.0;
+    c.a0[p] = a0;
+    c.b0[p] = b0;
     u_prev = u;
     sg_prev = sg;
   }

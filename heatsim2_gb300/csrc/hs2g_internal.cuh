@@ -14,20 +14,20 @@ struct Dims {
   __host__ __device__ int64_t nxy() const { return ny * nx; }
 };
 
-// Per-voxel coefficients of the scaled delta-form Douglas step, structure of arrays in voxel order.
+// Per-voxel coefficients of the scaled delta-form Douglas step.
 //   stage 0 (x lines):  z_i = wc*T + wxl*T[i-1] + wxh*T[i+1] + wyl*T[j-1] + wyh*T[j+1] + wzl*T[k-1]
 //                             + wzh*T[k+1] + wq*Q - a0*z_{i-1};   W0_i = z_i - b0*W0_{i+1}
 //   stage 1 (y lines):  z_j = W0_j - a1*z_{j-1};                   W1_j = z_j - b1*W1_{j+1}
 //   stage 2 (z lines):  z_k = W1_k - a2*z_{k-1};                   dT_k = z_k - b2*dT_{k+1};  T' = T + dT
+// The eight stage-0 stencil coefficients are chunk-blocked: for x-line L = k*ny + j and 32-column chunk ch,
+// block (L*nchunks + ch) holds [wc, wxl, wxh, wyl, wyh, wzl, wzh, wq] x 32 columns (2 KB, zero-padded past
+// nx), so a warp's stencil reads one contiguous stream instead of eight.  The other coefficients are
+// (nz, ny, nx) arrays in voxel order.
+constexpr int kXBlockCoeffs = 8;
+enum XCoeff { kWc = 0, kWxl, kWxh, kWyl, kWyh, kWzl, kWzh, kWq };
 struct Coeffs {
-  double* wc;
-  double* wxl;
-  double* wxh;
-  double* wyl;
-  double* wyh;
-  double* wzl;
-  double* wzh;
-  double* wq;
+  double* xb;   // stage-0 stencil blocks, nz*ny*nchunks*8*32 doubles
+  int64_t nchunks;
   double* a0;
   double* b0;
   double* a1;
@@ -35,7 +35,7 @@ struct Coeffs {
   double* a2;
   double* b2;
 };
-constexpr int kNumCoeffArrays = 14;
+constexpr int kNumCoeffArrays = 6;  // voxel-order arrays besides xb
 
 struct QTable {
   double q[HS2G_MAX_CLASSES];
@@ -70,7 +70,20 @@ struct StepArgs {
   const uint8_t* vclass;
   const double* qdense;  // may be null
   bool has_qtab;
+  int* status;           // device word: 0, or HS2G_ERR_TIMEOUT when a bounded wait in a kernel ran out
+  bool bulk_y, bulk_z;   // use the TMA tensor-tile line sweeps (hs2g_lines.cu) for y / z
+  struct TensorMapCache* tmaps;
 };
+
+// TMA tensor-tile line sweeps (hs2g_lines.cu); axis 1 = y, 2 = z.
+struct TensorMapCache;
+TensorMapCache* tensor_map_cache_create();
+void tensor_map_cache_destroy(TensorMapCache* c);
+bool lines_bulk_supported(const Dims& d, int axis);
+cudaError_t lines_bulk_prepare();
+cudaError_t launch_lines_bulk(const Dims& d, int axis, const double* A, const double* alpha, double* scratch,
+                              const double* beta, const double* T_in, double* out, int* status,
+                              TensorMapCache* cache, cudaStream_t s);
 cudaError_t launch_step(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s);
 // the same three kernels with an event recorded before each and after the last (ev[0..3])
 cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s,

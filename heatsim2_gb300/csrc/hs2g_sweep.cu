@@ -7,14 +7,15 @@
 // arranged for the fewest FP64 operations: 7 stencil FMAs (+1 when a source is active) and 2 recurrence
 // FMAs per voxel in the x sweep, 2 FMAs per voxel in the y sweep, 2 FMAs and 1 add per voxel in the z sweep.
 //
-// Memory layout: every array is (nz, ny, nx) with x fastest.
+// Memory layout: every field is (nz, ny, nx) with x fastest; the stage-0 stencil coefficients are
+// chunk-blocked (hs2g_internal.cuh).
 //   x sweep: a CTA owns 32 consecutive x-lines.  The stencil is evaluated in 32-column chunks with lanes
-//            along x (coalesced loads of T and the coefficients), staged through shared memory, and one warp
-//            runs the line recurrences down the transposed chunk (lane = line).  The forward values are kept
-//            in the output array W0 and re-read by the back substitution in the same CTA.
-//   y sweep: one thread per y-line (k,i); neighbouring lanes have neighbouring i, so each j step is one
-//            coalesced 256-byte load per array per warp.
-//   z sweep: one thread per z-line (j,i), same coalescing argument with stride ny*nx.
+//            along x (coalesced loads of T and of the line's coefficient block), staged through shared memory,
+//            and one warp runs the 32 line recurrences down the transposed chunk (lane = line).  The forward
+//            values are kept in the output array W0 and re-read by the back substitution in the same CTA.
+//   y sweep: TMA tensor tiles (hs2g_lines.cu), or one thread per y-line with plain loads.
+//   z sweep: one thread per z-line (j,i); neighbouring lanes have neighbouring i, so each k step is one
+//            coalesced 256-byte access per array per warp (a TMA variant exists, HS2G_Z_SWEEP=tma).
 #include "hs2g_internal.cuh"
 
 namespace hs2g {
@@ -26,6 +27,41 @@ constexpr int kXThreads = 128;
 constexpr int kXWarps = kXThreads / 32;
 constexpr int kXLinesPerWarp = kXLines / kXWarps;
 constexpr int kLineThreads = 128;
+
+// Stage-0 right-hand side of voxel (L, i) of x-line L = k*ny + j, pre-scaled by the line's pivot:
+// wc*T + wxl*T[i-1] + wxh*T[i+1] + wyl*T[j-1] + wyh*T[j+1] + wzl*T[k-1] + wzh*T[k+1] (+ wq*Q).
+// Out-of-grid neighbours carry a zero coefficient (exterior faces are insulating): T[p] is read instead.
+// Column i = ch*32 + lane of the chunk; the coefficients come from the line's chunk block.
+template <bool HAS_Q>
+__device__ __forceinline__ double stencil_x(const Dims& d, const double* __restrict__ T, const Coeffs& c,
+                                            const uint8_t* __restrict__ vclass, const double* __restrict__ qdense,
+                                            const double* sq, int64_t L, int ch, int lane) {
+  const int64_t i = (int64_t)ch * 32 + lane;
+  const int64_t k = L / d.ny, j = L - k * d.ny;
+  const int64_t p = L * d.nx + i;
+  const int64_t nxy = d.nxy();
+  const double* __restrict__ w = c.xb + ((L * c.nchunks + ch) * kXBlockCoeffs) * 32 + lane;
+  const double t = T[p];
+  const double txl = i > 0 ? T[p - 1] : t;
+  const double txh = i + 1 < d.nx ? T[p + 1] : t;
+  const double tyl = j > 0 ? T[p - d.nx] : t;
+  const double tyh = j + 1 < d.ny ? T[p + d.nx] : t;
+  const double tzl = k > 0 ? T[p - nxy] : t;
+  const double tzh = k + 1 < d.nz ? T[p + nxy] : t;
+  double r = w[kWc * 32] * t;
+  r = fma(w[kWxl * 32], txl, r);
+  r = fma(w[kWxh * 32], txh, r);
+  r = fma(w[kWyl * 32], tyl, r);
+  r = fma(w[kWyh * 32], tyh, r);
+  r = fma(w[kWzl * 32], tzl, r);
+  r = fma(w[kWzh * 32], tzh, r);
+  if (HAS_Q) {
+    double q = sq[vclass[p]];
+    if (qdense) q += qdense[p];
+    r = fma(w[kWq * 32], q, r);
+  }
+  return r;
+}
 
 template <bool HAS_Q>
 __global__ void __launch_bounds__(kXThreads) sweep_x_kernel(Dims d, const double* __restrict__ T, Coeffs c,
@@ -41,7 +77,6 @@ __global__ void __launch_bounds__(kXThreads) sweep_x_kernel(Dims d, const double
   }
   const int64_t nlines = d.nz * d.ny;
   const int64_t L0 = (int64_t)blockIdx.x * kXLines;
-  const int64_t nxy = d.nxy();
   const int nchunks = (int)((d.nx + kXChunk - 1) / kXChunk);
   __syncthreads();
 
@@ -55,29 +90,8 @@ __global__ void __launch_bounds__(kXThreads) sweep_x_kernel(Dims d, const double
       const int64_t L = L0 + l;
       double r = 0.0, a = 0.0;
       if (L < nlines && i < d.nx) {
-        const int64_t k = L / d.ny, j = L - k * d.ny;
-        const int64_t p = L * d.nx + i;
-        const double t = T[p];
-        // out-of-grid neighbours carry a zero coefficient (exterior faces are insulating): read T[p] instead
-        const double txl = i > 0 ? T[p - 1] : t;
-        const double txh = i + 1 < d.nx ? T[p + 1] : t;
-        const double tyl = j > 0 ? T[p - d.nx] : t;
-        const double tyh = j + 1 < d.ny ? T[p + d.nx] : t;
-        const double tzl = k > 0 ? T[p - nxy] : t;
-        const double tzh = k + 1 < d.nz ? T[p + nxy] : t;
-        r = c.wc[p] * t;
-        r = fma(c.wxl[p], txl, r);
-        r = fma(c.wxh[p], txh, r);
-        r = fma(c.wyl[p], tyl, r);
-        r = fma(c.wyh[p], tyh, r);
-        r = fma(c.wzl[p], tzl, r);
-        r = fma(c.wzh[p], tzh, r);
-        if (HAS_Q) {
-          double q = sq[vclass[p]];
-          if (qdense) q += qdense[p];
-          r = fma(c.wq[p], q, r);
-        }
-        a = c.a0[p];
+        r = stencil_x<HAS_Q>(d, T, c, vclass, qdense, sq, L, ch, lane);
+        a = c.a0[L * d.nx + i];
       }
       sr[l][lane] = r;
       sa[l][lane] = a;
@@ -254,10 +268,19 @@ cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable&
   else
     sweep_x_kernel<false><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0);
   if (ev) cudaEventRecord(ev[1], s);
-  sweep_y_kernel<<<blocks(d.nz * d.nx, kLineThreads), kLineThreads, 0, s>>>(d, a.W0, c.a1, c.b1, a.W1);
+  cudaError_t e = cudaSuccess;
+  if (a.bulk_y)
+    e = launch_lines_bulk(d, 1, a.W0, c.a1, a.W1, c.b1, nullptr, a.W1, a.status, a.tmaps, s);
+  else
+    sweep_y_kernel<<<blocks(d.nz * d.nx, kLineThreads), kLineThreads, 0, s>>>(d, a.W0, c.a1, c.b1, a.W1);
+  if (e != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[2], s);
-  sweep_z_kernel<<<blocks(d.nxy(), kLineThreads), kLineThreads, 0, s>>>(d, a.W1, c.a2, c.b2, a.T_in, a.W0,
-                                                                         a.T_out);
+  if (a.bulk_z)
+    e = launch_lines_bulk(d, 2, a.W1, c.a2, a.W0, c.b2, a.T_in, a.T_out, a.status, a.tmaps, s);
+  else
+    sweep_z_kernel<<<blocks(d.nxy(), kLineThreads), kLineThreads, 0, s>>>(d, a.W1, c.a2, c.b2, a.T_in, a.W0,
+                                                                           a.T_out);
+  if (e != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[3], s);
   return cudaGetLastError();
 }

@@ -36,6 +36,7 @@ extern "C" {
 #define HS2G_ERR_FORM (-7)       /* a face flux is not a conservative Crank-Nicolson two-point difference */
 #define HS2G_ERR_CAPACITY (-8)   /* a computed voxel has rho*c/dt <= 0 or not finite */
 #define HS2G_ERR_STATE (-9)      /* handle not in a state that allows this call */
+#define HS2G_ERR_TIMEOUT (-10)   /* a bounded wait inside a kernel ran out; the step's output is invalid */
 
 /* flags */
 #define HS2G_DEVICE 1            /* T_in / T_out / qdense / history are device pointers (no copies) */
@@ -122,7 +123,8 @@ int hs2g_create_dense(const hs2g_dense_problem* problem, int device, hs2g_handle
 /* Free every device buffer of the handle (replaces delete_adi_step, alternatingdirection_c.c:14-54). */
 void hs2g_destroy(hs2g_handle* h);
 
-/* Queue subsequent work on `stream` (a cudaStream_t; NULL = the handle's own stream). */
+/* Queue subsequent work on `stream` (a cudaStream_t; NULL = the CUDA legacy default stream, as everywhere in
+   CUDA).  A new handle uses a non-blocking stream of its own until this is called. */
 int hs2g_set_stream(hs2g_handle* h, void* stream);
 int hs2g_shape(const hs2g_handle* h, int64_t shape[3]);
 

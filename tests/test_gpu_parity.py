@@ -119,6 +119,20 @@ def test_composite_panel_midsize_vs_oracle(cuda_ok):
     _compare_with_oracle(spec, 25)
 
 
+def test_bulk_copy_and_plain_line_sweeps_agree_bitwise(cuda_ok, monkeypatch):
+    """The TMA bulk-copy y/z sweeps (even row widths) and the plain-load sweeps do the same FMAs in the same
+    order, so their results are identical."""
+    spec = W.composite_panel(seed=5, nz=20, ny=70, nx=66, top_layers=6, width_range=(5, 30), depth_range=(2, 15))
+    outs = []
+    for y_mode, z_mode in (("tma", "plain"), ("plain", "tma"), ("plain", "plain")):
+        monkeypatch.setenv("HS2G_LINE_SWEEP", y_mode)
+        monkeypatch.setenv("HS2G_Z_SWEEP", z_mode)
+        P, S = _setup(spec)
+        outs.append(_run_host(spec, W.step_times(spec, 5), P, S)[5])
+    np.testing.assert_array_equal(outs[0], outs[1])
+    np.testing.assert_array_equal(outs[0], outs[2])
+
+
 def test_uneven_instances_vs_oracle(cuda_ok):
     for spec in W.uneven_batch(seed=2, n=3, nz_range=(16, 24), nxy_range=(40, 70)):
         _compare_with_oracle(spec, 6)
