@@ -25,7 +25,8 @@ MAX_CLASSES = 256
 
 EXPORTED = ("hs2g_abi_version", "hs2g_last_error", "hs2g_create_classes", "hs2g_create_dense", "hs2g_destroy",
             "hs2g_set_stream", "hs2g_shape", "hs2g_step", "hs2g_run", "hs2g_source_table", "hs2g_get_faces",
-            "hs2g_device_bytes", "hs2g_run_timed", "hs2g_fp64_fma_rate")
+            "hs2g_device_bytes", "hs2g_run_timed", "hs2g_fp64_fma_rate", "hs2g_step_static")
+STATIC_MAX_VOXELS = 1 << 20
 
 
 class NativeLibraryError(RuntimeError):
@@ -109,6 +110,8 @@ def load():
         L.hs2g_run_timed.restype = i32
         L.hs2g_fp64_fma_rate.argtypes = [i32, vp]
         L.hs2g_fp64_fma_rate.restype = i32
+        L.hs2g_step_static.argtypes = [i64, i64, i64, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.hs2g_step_static.restype = i32
         L.hs2g_device_bytes.argtypes = [vp]
         L.hs2g_device_bytes.restype = i64
         if L.hs2g_abi_version() != ABI_VERSION:

@@ -251,6 +251,8 @@ int ensure_staging(hs2g_handle* h) {
 
 }  // namespace
 
+int hs2g::set_last_error(int code, const char* message) { return fail(code, "%s", message); }
+
 extern "C" {
 
 int hs2g_abi_version(void) { return HS2G_ABI_VERSION; }

@@ -41,6 +41,9 @@ struct QTable {
   double q[HS2G_MAX_CLASSES];
 };
 
+// Record the message hs2g_last_error() returns for this thread (hs2g_api.cu); returns code.
+int set_last_error(int code, const char* message);
+
 // First error recorded by a device kernel: (code << 56) | (axis << 54) | index, 0 when none.
 __device__ __forceinline__ void record_error(unsigned long long* err, int code, int axis, int64_t index) {
   unsigned long long v = ((unsigned long long)(-code) << 56) | ((unsigned long long)axis << 54) |

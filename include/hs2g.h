@@ -167,6 +167,29 @@ int hs2g_fp64_fma_rate(int device, double* fma_per_s);
 int hs2g_source_table(int nsrc, const int32_t* kind, const double* params, double t, double dt, double volume,
                       double* qtab);
 
+/*
+ * One timestep that allocates nothing: no counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory -- a plugin whose host application owns every device
+ * allocation and forbids its plugins from calling cudaMalloc (a fixed device-memory budget, or a pool
+ * allocator that must not be bypassed).  Such callers cannot create a handle, so this call takes the problem
+ * itself in caller-owned device memory: face conductances Gz (nz+1,ny,nx), Gy (nz,ny+1,nx), Gx (nz,ny,nx+1)
+ * in W/m^3/K, capacities rho*c/dt (nz,ny,nx), the fixed-temperature mask (or NULL), the per-voxel source in
+ * W/m^3 (or NULL) and T_in; it writes T_out (which may equal T_in).  Faces on the grid's exterior are treated
+ * as insulating.  Each line is factorised as it is swept, so the call does more FP64 work per step than
+ * hs2g_step on a compiled handle.
+ *
+ * The intermediate fields live in a static device array sized for HS2G_STATIC_MAX_VOXELS voxels (24 MiB),
+ * held by every GPU that loads the library until the process exits; larger grids return HS2G_ERR_ARG.
+ * Every call shares that array: calls that overlap on the GPU race and must be serialised by the caller.
+ * The first call on a device takes the array's device address (cudaGetSymbolAddress); make it before any
+ * stream capture.  Work is queued on `stream` (a cudaStream_t, NULL = default stream); no synchronisation.
+ */
+#define HS2G_STATIC_MAX_VOXELS (1 << 20)
+int hs2g_step_static(int64_t nz, int64_t ny, int64_t nx, const double* Gz, const double* Gy, const double* Gx,
+                     const double* capacity, const uint8_t* fixed, const double* Q, const double* T_in,
+                     double* T_out, void* stream);
+
 /* Copy the compiled face conductances and capacities to host buffers (any may be NULL). */
 int hs2g_get_faces(hs2g_handle* h, double* Gz, double* Gy, double* Gx, double* capacity, uint8_t* fixed);
 
