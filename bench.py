@@ -371,8 +371,9 @@ def gpu_arm(args, world, rank, local_rank):
                                    "anisotropic composite over aluminium, 3 delaminations, flash at t=0, dt=5 ms"
                                    % tuple(args.shape),
                        "grid": [nz, ny, nx], "computed_voxels": compute_vox, "seed": SEED,
-                       "l2": "inputs larger than L2 (T %.0f MB + step coefficients %.0f MB)"
-                             % (grid_vox * 8 / 1e6, grid_vox * 8 * 14 / 1e6),
+                       "l2": "inputs larger than L2 (T %.0f MB, device state %.0f MB)"
+                             % (grid_vox * 8 / 1e6, P.device_bytes / 1e6),
+                       "kernels": "x: CTA-staged stencil + warp recurrence; y: TMA tensor-tile ring; z: per-line",
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": roofline, "fp64_roofline": fp64,
             "kernel_ms_per_step": per_kernel_ms, "kernel_fp64_frac": per_kernel_fp64,
