@@ -52,6 +52,9 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-instances", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=100)
     ap.add_argument("--cpu-worker", default=None, help=argparse.SUPPRESS)
     return ap.parse_args()
 
@@ -262,6 +265,84 @@ def reference_arm(args, world, rank):
 
 
 # ------------------------------------------------------------------------------------------------------------
+# batched form (uneven instances) against a loop of the single-problem path
+# ------------------------------------------------------------------------------------------------------------
+def batched_measurement(args, world, rank, dev):
+    """256 uneven instances (nz 16..64, ny,nx 64..256; steel or composite; one flaw; flash), seed 2.
+    FP64 and FP32 batches (autotuned, one CUDA graph per step) against a per-instance loop of hs2g_run."""
+    import ctypes
+    import numpy as np
+    import torch
+    import heatsim2_gb300 as hs
+    from heatsim2_gb300 import _native, workloads as W
+    from heatsim2_gb300.batch import Batch, shard
+    from heatsim2_gb300.alternatingdirection import _ClassSources, source_table
+
+    L = _native.load()
+    specs_all = W.uneven_batch(seed=2, n=args.batch_instances)
+    sizes = [W.voxels(s) for s in specs_all]
+    specs = [specs_all[i] for i in shard(sizes, world, rank)]
+    steps = args.batch_steps
+    dt = specs[0]["dt"]
+    times = W.step_times(specs[0], steps)
+    computed = sum(s.get("compute_voxels", W.voxels(s)) for s in specs)
+    out = {"workload": "%d uneven instances (seed 2), %d steps of dt=%g" % (len(specs_all), steps, dt),
+           "instances": len(specs), "computed_voxels": computed}
+    results = {}
+    for prec in (64, 32):
+        t0 = time.perf_counter()
+        b = Batch([W.setup_args(hs, s) for s in specs], precision=prec)
+        setup_s = time.perf_counter() - t0
+        b.set_temperature([W.initial_temperature(s) for s in specs])
+        tune = b.autotune()
+        b.set_sources(times, dt)
+        b.run(0)
+        torch.cuda.synchronize()
+        ms = b.run(steps)
+        results[prec] = b.get_temperature()
+        out["fp%d" % prec] = {"value": computed * steps / (ms * 1e-3), "ms_per_step": ms / steps,
+                              "setup_s": setup_s, "device_bytes": b.device_bytes,
+                              "tuning": tune.strip().splitlines()[-1]}
+        del b
+    out["fp32_max_rel_err_vs_fp64"] = max(
+        float(np.abs(a - c).max() / np.abs(a).max()) for a, c in zip(results[64], results[32]))
+    # per-instance loop of the single-problem path on the same instances, one stream, device time
+    handles = []
+    for s in specs:
+        P, S = hs.setup(*W.setup_args(hs, s))
+        src = _ClassSources(W.volumetric_tuple(hs, s))
+        q = np.ascontiguousarray([source_table(src, t, dt, P.volume_array)[0] for t in times])
+        T = torch.from_numpy(W.initial_temperature(s)).to(dev)
+        handles.append((P, q, T))
+    stream = torch.cuda.Stream(device=dev)
+    for P, _, _ in handles:
+        _native.check(L.hs2g_set_stream(P.handle.ptr, ctypes.c_void_p(stream.cuda_stream)))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for P, q, T in handles:
+        _native.check(L.hs2g_run(P.handle.ptr, steps, T.data_ptr(), T.data_ptr(), q.ctypes.data, 0, None,
+                                 _native.DEVICE))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    loop_ms = e0.elapsed_time(e1)
+    worst = max(float(np.abs(T.cpu().numpy() - r).max() / np.abs(r).max())
+                for (_, _, T), r in zip(handles, results[64]))
+    out["plain_loop"] = {"value": computed * steps / (loop_ms * 1e-3), "ms_per_step": loop_ms / steps,
+                         "max_rel_diff_vs_batch_fp64": worst}
+    if world > 1:
+        for key in ("fp64", "fp32", "plain_loop"):
+            t = torch.tensor([out[key]["ms_per_step"]], device=dev, dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            c = torch.tensor([float(computed)], device=dev, dtype=torch.float64)
+            torch.distributed.all_reduce(c)
+            out[key]["value"] = float(c.item()) / (float(t.item()) * 1e-3)
+    out["speedup_fp64_vs_loop"] = out["fp64"]["value"] / out["plain_loop"]["value"]
+    del handles
+    return out
+
+
+# ------------------------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------------------------
 def gpu_arm(args, world, rank, local_rank):
@@ -359,6 +440,12 @@ def gpu_arm(args, world, rank, local_rank):
         e2e = {"value": world * compute_vox * E / el, "unit": METRIC, "h2d_bytes_per_step": grid_vox * 8,
                "d2h_bytes_per_step": grid_vox * 8, "steps": E,
                "path": "hs2g_step with pinned host buffers (copy in, 3 sweeps, copy out, sync) per step"}
+    state_bytes = P.device_bytes
+    batched = None
+    if not args.no_batched:
+        del P, S
+        torch.cuda.empty_cache()
+        batched = batched_measurement(args, world, rank, dev)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = run_cpu_baseline(args.cpu_seconds)
@@ -372,14 +459,14 @@ def gpu_arm(args, world, rank, local_rank):
                                    % tuple(args.shape),
                        "grid": [nz, ny, nx], "computed_voxels": compute_vox, "seed": SEED,
                        "l2": "inputs larger than L2 (T %.0f MB, device state %.0f MB)"
-                             % (grid_vox * 8 / 1e6, P.device_bytes / 1e6),
+                             % (grid_vox * 8 / 1e6, state_bytes / 1e6),
                        "kernels": "x: CTA-staged stencil + warp recurrence; y: TMA tensor-tile ring; z: per-line",
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": roofline, "fp64_roofline": fp64,
             "kernel_ms_per_step": per_kernel_ms, "kernel_fp64_frac": per_kernel_fp64,
             "kernel_hbm_frac": per_kernel_hbm,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * K, "clocks": clk, "setup_s": setup_s,
-            "device_bytes": P.device_bytes,
+            "device_bytes": state_bytes, "batched": batched,
         }
         print(json.dumps(line), flush=True)
 

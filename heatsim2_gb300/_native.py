@@ -25,7 +25,10 @@ MAX_CLASSES = 256
 
 EXPORTED = ("hs2g_abi_version", "hs2g_last_error", "hs2g_create_classes", "hs2g_create_dense", "hs2g_destroy",
             "hs2g_set_stream", "hs2g_shape", "hs2g_step", "hs2g_run", "hs2g_source_table", "hs2g_get_faces",
-            "hs2g_device_bytes", "hs2g_run_timed", "hs2g_fp64_fma_rate", "hs2g_step_static")
+            "hs2g_device_bytes", "hs2g_run_timed", "hs2g_fp64_fma_rate", "hs2g_step_static",
+            "hs2g_batch_create", "hs2g_batch_destroy", "hs2g_batch_layout", "hs2g_batch_device_bytes",
+            "hs2g_batch_set_temperature", "hs2g_batch_get_temperature", "hs2g_batch_set_sources",
+            "hs2g_batch_set_clock", "hs2g_batch_run", "hs2g_batch_autotune")
 STATIC_MAX_VOXELS = 1 << 20
 
 
@@ -112,6 +115,26 @@ def load():
         L.hs2g_fp64_fma_rate.restype = i32
         L.hs2g_step_static.argtypes = [i64, i64, i64, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.hs2g_step_static.restype = i32
+        L.hs2g_batch_create.argtypes = [i32, ctypes.POINTER(ClassProblem), i32, i32, ctypes.POINTER(vp)]
+        L.hs2g_batch_create.restype = i32
+        L.hs2g_batch_destroy.argtypes = [vp]
+        L.hs2g_batch_destroy.restype = None
+        L.hs2g_batch_layout.argtypes = [vp, vp, vp]
+        L.hs2g_batch_layout.restype = i32
+        L.hs2g_batch_device_bytes.argtypes = [vp]
+        L.hs2g_batch_device_bytes.restype = i64
+        L.hs2g_batch_set_temperature.argtypes = [vp, vp, i32]
+        L.hs2g_batch_set_temperature.restype = i32
+        L.hs2g_batch_get_temperature.argtypes = [vp, vp, i32]
+        L.hs2g_batch_get_temperature.restype = i32
+        L.hs2g_batch_set_sources.argtypes = [vp, i32, i32, vp]
+        L.hs2g_batch_set_sources.restype = i32
+        L.hs2g_batch_set_clock.argtypes = [vp, i32]
+        L.hs2g_batch_set_clock.restype = i32
+        L.hs2g_batch_run.argtypes = [vp, i32, i32, ctypes.POINTER(dp)]
+        L.hs2g_batch_run.restype = i32
+        L.hs2g_batch_autotune.argtypes = [vp, ctypes.c_char_p, i32]
+        L.hs2g_batch_autotune.restype = i32
         L.hs2g_device_bytes.argtypes = [vp]
         L.hs2g_device_bytes.restype = i64
         if L.hs2g_abi_version() != ABI_VERSION:

@@ -190,6 +190,52 @@ class _Handle(object):
             self.ptr = None
 
 
+class ClassProblem(object):
+    """A validated problem packed for the C ABI (hs2g_class_problem); keeps its arrays alive."""
+
+    def __init__(self, z0, y0, x0, dz, dy, dx, nz, ny, nx, dt, materials, boundaries, volumetric,
+                 material_elements, boundary_z_elements, boundary_y_elements, boundary_x_elements,
+                 volumetric_elements, top_surface_y_curvatures=None, top_surface_x_curvatures=None,
+                 unaligned_anisotropic=False):
+        if top_surface_y_curvatures is not None or top_surface_x_curvatures is not None:
+            raise NotImplementedError("the curved top-surface mode (crank_nicolson.pyx:388-457) is not provided")
+        if unaligned_anisotropic:
+            raise NotImplementedError("the unaligned-anisotropic ADI mode (alternatingdirection_c_pyx.pyx:511-564) "
+                                      "is not provided")
+        nz, ny, nx = int(nz), int(ny), int(nx)
+        if nz < 1 or ny < 1 or nx < 1:
+            raise ValueError("grid dimensions must be positive")
+        if not (dt > 0 and math.isfinite(dt)):
+            raise ValueError("dt must be positive")
+        if len(materials) > _native.MAX_CLASSES or len(boundaries) > _native.MAX_CLASSES:
+            raise ValueError("at most 256 material and boundary classes (uint8 class arrays)")
+        self.shape = (nz, ny, nx)
+        self.spacing = (dz, dy, dx)
+        self.origin = (z0, y0, x0)
+        self.dt = dt
+        self.volumetric = volumetric
+        self.mat = _u8_array(material_elements, "material_elements", (nz, ny, nx))
+        self.bz = _u8_array(boundary_z_elements, "boundary_z_elements", (nz + 1, ny, nx))
+        self.by = _u8_array(boundary_y_elements, "boundary_y_elements", (nz, ny + 1, nx))
+        self.bx = _u8_array(boundary_x_elements, "boundary_x_elements", (nz, ny, nx + 1))
+        self.vol = _u8_array(volumetric_elements, "volumetric_elements", (nz, ny, nx))
+        self.mats = compile_materials(materials, dt)
+        self.forms = compile_boundary_forms(boundaries, dz, dy, dx)
+        self.struct = _native.ClassProblem(nz, ny, nx, len(materials), len(boundaries), self.mats, self.forms,
+                                           self.mat.ctypes.data, self.bz.ctypes.data, self.by.ctypes.data,
+                                           self.bx.ctypes.data, self.vol.ctypes.data)
+
+
+def raise_compile_error(rc):
+    """Map an hs2g compile error code to the exception the reference raises in that situation."""
+    L = _native.load()
+    if rc == _native.ERR_UNALIGNED:
+        raise UnalignedAnisotropyError(L.hs2g_last_error().decode())
+    if rc in (_native.ERR_EXTERIOR, _native.ERR_KTYPE, _native.ERR_FORM, _native.ERR_CAPACITY, _native.ERR_ARG):
+        raise ValueError(L.hs2g_last_error().decode())
+    _native.check(rc)
+
+
 def setup(z0, y0, x0, dz, dy, dx, nz, ny, nx, dt, materials, boundaries, volumetric, material_elements,
           boundary_z_elements, boundary_y_elements, boundary_x_elements, volumetric_elements,
           top_surface_y_curvatures=None, top_surface_x_curvatures=None, unaligned_anisotropic=False):
@@ -198,38 +244,19 @@ def setup(z0, y0, x0, dz, dy, dx, nz, ny, nx, dt, materials, boundaries, volumet
     Arguments as in the reference (crank_nicolson.pyx:128-142).  The curved-surface mode and the
     unaligned-anisotropic 15-stage mode are not provided (NotImplementedError)."""
     from .alternatingdirection import adi_params, adi_step
-    if top_surface_y_curvatures is not None or top_surface_x_curvatures is not None:
-        raise NotImplementedError("the curved top-surface mode (crank_nicolson.pyx:388-457) is not provided")
-    if unaligned_anisotropic:
-        raise NotImplementedError("the unaligned-anisotropic ADI mode (alternatingdirection_c_pyx.pyx:511-564) "
-                                  "is not provided")
-    nz, ny, nx = int(nz), int(ny), int(nx)
-    if nz < 1 or ny < 1 or nx < 1:
-        raise ValueError("grid dimensions must be positive")
-    if not (dt > 0 and math.isfinite(dt)):
-        raise ValueError("dt must be positive")
-    if len(materials) > _native.MAX_CLASSES or len(boundaries) > _native.MAX_CLASSES:
-        raise ValueError("at most 256 material and boundary classes (uint8 class arrays)")
-    mat = _u8_array(material_elements, "material_elements", (nz, ny, nx))
-    bz = _u8_array(boundary_z_elements, "boundary_z_elements", (nz + 1, ny, nx))
-    by = _u8_array(boundary_y_elements, "boundary_y_elements", (nz, ny + 1, nx))
-    bx = _u8_array(boundary_x_elements, "boundary_x_elements", (nz, ny, nx + 1))
-    vol = _u8_array(volumetric_elements, "volumetric_elements", (nz, ny, nx))
-    mats = compile_materials(materials, dt)
-    forms = compile_boundary_forms(boundaries, dz, dy, dx)
+    cp = ClassProblem(z0, y0, x0, dz, dy, dx, nz, ny, nx, dt, materials, boundaries, volumetric, material_elements,
+                      boundary_z_elements, boundary_y_elements, boundary_x_elements, volumetric_elements,
+                      top_surface_y_curvatures, top_surface_x_curvatures, unaligned_anisotropic)
+    nz, ny, nx = cp.shape
     L = _native.load()
-    prob = _native.ClassProblem(nz, ny, nx, len(materials), len(boundaries), mats, forms,
-                                mat.ctypes.data, bz.ctypes.data, by.ctypes.data, bx.ctypes.data, vol.ctypes.data)
     device = current_device()
     import ctypes
     h = ctypes.c_void_p()
-    rc = L.hs2g_create_classes(ctypes.byref(prob), device, ctypes.byref(h))
-    if rc == _native.ERR_UNALIGNED:
-        raise UnalignedAnisotropyError(L.hs2g_last_error().decode())
-    if rc in (_native.ERR_EXTERIOR, _native.ERR_KTYPE, _native.ERR_FORM, _native.ERR_CAPACITY, _native.ERR_ARG):
-        raise ValueError(L.hs2g_last_error().decode())
-    _native.check(rc)
+    rc = L.hs2g_create_classes(ctypes.byref(cp.struct), device, ctypes.byref(h))
+    if rc != _native.OK:
+        raise_compile_error(rc)
     handle = _Handle(h, device)
+    vol = cp.vol
     params = adi_params(shape=(nz, ny, nx), volume_array=dz * dy * dx, dt=dt, handle=handle, device=device,
                         spacing=(dz, dy, dx), origin=(z0, y0, x0), compiled_volumetric=vol.copy())
     steps = tuple(adi_step(params, perm, s) for s, perm in enumerate(((0, 1, 2), (2, 0, 1), (1, 2, 0))))

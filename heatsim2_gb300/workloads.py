@@ -159,10 +159,12 @@ def steel_slab(seed=0, nz=20, ny=40, nx=40, d=1e-3, dt=0.01, nsteps=200, h=1000.
     a = _zero_arrays(nz, ny, nx)
     # boundary classes: 0 conducting, 1 insulating, 2 thin layer
     _insulate_exterior(a, 1)
-    depth = int(rng.integers(depth_range[0], depth_range[1] + 1))
+    hi = min(depth_range[1], nz - 1)          # an interior z-face (the exterior ones must stay insulating)
+    depth = int(rng.integers(min(depth_range[0], hi), hi + 1)) if hi >= 1 else 0
     y0 = int(rng.integers(0, ny - flaw + 1))
     x0 = int(rng.integers(0, nx - flaw + 1))
-    a["boundary_z"][depth, y0:y0 + flaw, x0:x0 + flaw] = 2
+    if depth >= 1:
+        a["boundary_z"][depth, y0:y0 + flaw, x0:x0 + flaw] = 2
     a["volumetric"][0] = 1
     return {
         "name": "steel_slab", "grid": _grid(nz, ny, nx, d), "dt": dt, "t0": 0.0, "nsteps": nsteps,
@@ -199,11 +201,12 @@ def composite_panel(seed=1, nz=64, ny=512, nx=512, d=0.5e-3, dt=0.005, nsteps=10
     a["boundary_z"][1] = 2
     delams = []
     dmax = min(depth_range[1], nz - 1)
-    for _ in range(n_delams):
+    dmin = min(depth_range[0], dmax)
+    for _ in range(n_delams if dmax >= 1 else 0):
         wy = int(rng.integers(width_range[0], width_range[1] + 1))
         wx = int(rng.integers(width_range[0], width_range[1] + 1))
         wy, wx = min(wy, ny), min(wx, nx)
-        depth = int(rng.integers(depth_range[0], dmax + 1))
+        depth = int(rng.integers(dmin, dmax + 1))
         y0 = int(rng.integers(0, ny - wy + 1))
         x0 = int(rng.integers(0, nx - wx + 1))
         a["boundary_z"][1 + depth, y0:y0 + wy, x0:x0 + wx] = 1

@@ -190,6 +190,35 @@ int hs2g_step_static(int64_t nz, int64_t ny, int64_t nx, const double* Gz, const
                      const double* capacity, const uint8_t* fixed, const double* Q, const double* T_in,
                      double* T_out, void* stream);
 
+/*
+ * Batched form: n independent problems of uneven size advanced together (no counterpart in the reference,
+ * whose time loop handles one problem; a loop over run_adi_steps calls is what it replaces).  All instances
+ * live in one concatenated state: instance i's (nz_i, ny_i, nx_i) field starts at voxel offsets[i] (see
+ * hs2g_batch_layout).  precision 64 stores and computes in double (per instance equal to hs2g_step bit for
+ * bit); precision 32 compiles in double and stores / sweeps in float.  A timestep is three persistent sweep
+ * kernels over flattened line lists, captured once in a CUDA graph and replayed.
+ */
+typedef struct hs2g_batch hs2g_batch;
+int hs2g_batch_create(int n, const hs2g_class_problem* problems, int precision, int device, hs2g_batch** out);
+void hs2g_batch_destroy(hs2g_batch* b);
+/* offsets[n+1] voxel offsets of the instances, dims[n][3] their (nz, ny, nx); either may be NULL. */
+int hs2g_batch_layout(const hs2g_batch* b, int64_t* offsets, int64_t* dims);
+int64_t hs2g_batch_device_bytes(const hs2g_batch* b);
+/* Temperature of all instances, concatenated (offsets[n] doubles), host or device (HS2G_DEVICE).  With
+   precision 32, pass temperatures as offsets from an ambient value (the step maps a uniform field to itself,
+   so offsets evolve exactly like temperatures) to spend float resolution on the changes. */
+int hs2g_batch_set_temperature(hs2g_batch* b, const double* T, int flags);
+int hs2g_batch_get_temperature(hs2g_batch* b, double* T, int flags);
+/* Source schedule: qtabs[nsteps][n][nclass] per-class source values (W/m^3) of every instance at every step
+   (host); resets the step clock to 0.  Steps beyond the schedule have no source. */
+int hs2g_batch_set_sources(hs2g_batch* b, int nsteps, int nclass, const double* qtabs);
+int hs2g_batch_set_clock(hs2g_batch* b, int step);
+/* Advance every instance by nsteps (graph replays on the batch's stream).  elapsed_ms (or NULL) receives the
+   device time of the replays measured with CUDA events; HS2G_SYNC waits for completion. */
+int hs2g_batch_run(hs2g_batch* b, int nsteps, int flags, double* elapsed_ms);
+/* Time candidate launch shapes per axis on this batch and keep the fastest; writes a report. */
+int hs2g_batch_autotune(hs2g_batch* b, char* report, int report_len);
+
 /* Copy the compiled face conductances and capacities to host buffers (any may be NULL). */
 int hs2g_get_faces(hs2g_handle* h, double* Gz, double* Gy, double* Gx, double* capacity, uint8_t* fixed);
 

@@ -1,0 +1,77 @@
+"""Batched form (heatsim2_gb300.batch.Batch): uneven instances advanced together must give, instance by
+instance, the single-problem result (FP64: bit for bit, the same FMAs in the same order), and the FP32 variant
+stays within its stated error of FP64."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+import heatsim2_gb300 as hs
+from heatsim2_gb300 import workloads as W
+from heatsim2_gb300.batch import Batch
+
+pytestmark = pytest.mark.gpu
+
+
+def _instances():
+    return [
+        W.steel_slab(seed=11, nz=7, ny=13, nx=10, flaw=4, depth_range=(2, 4), nsteps=6),
+        W.composite_panel(seed=12, nz=9, ny=20, nx=33, top_layers=3, n_delams=2, width_range=(3, 9),
+                          depth_range=(2, 6), nsteps=6),
+        W.steel_slab(seed=13, nz=5, ny=34, nx=71, flaw=6, depth_range=(1, 3), nsteps=6),
+        W.composite_panel(seed=14, nz=12, ny=9, nx=40, top_layers=4, n_delams=1, width_range=(3, 7),
+                          depth_range=(2, 8), nsteps=6),
+        W.line_grid((1, 1, 9)),
+    ]
+
+
+def _single(spec, nsteps):
+    P, S = hs.setup(*W.setup_args(hs, spec))
+    vol = W.volumetric_tuple(hs, spec)
+    T = W.initial_temperature(spec)
+    for t in W.step_times(spec, nsteps):
+        T = hs.run_adi_steps(P, S, t, spec["dt"], T, spec["arrays"]["volumetric"], vol)
+    return T
+
+
+def _batch(specs, nsteps, precision=64, tune=False, split=None):
+    b = Batch([W.setup_args(hs, s) for s in specs], precision=precision)
+    b.set_temperature([W.initial_temperature(s) for s in specs])
+    b.set_sources(W.step_times(specs[0], nsteps), specs[0]["dt"])
+    if tune:
+        b.autotune()
+    if split:
+        b.run(split)
+        b.run(nsteps - split)
+    else:
+        b.run(nsteps)
+    return b.get_temperature()
+
+
+def test_batch_fp64_equals_single_problem_path(cuda_ok):
+    specs = _instances()
+    for s in specs:
+        s["dt"] = 0.01      # one source schedule for the batch
+    got = _batch(specs, 6)
+    for spec, T in zip(specs, got):
+        np.testing.assert_array_equal(T, _single(spec, 6))
+
+
+def test_batch_autotune_and_split_runs_keep_results(cuda_ok):
+    specs = _instances()
+    for s in specs:
+        s["dt"] = 0.01
+    a = _batch(specs, 5)
+    b = _batch(specs, 5, tune=True, split=2)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+
+
+def test_batch_fp32_error_against_fp64(cuda_ok):
+    specs = _instances()[:4]
+    for s in specs:
+        s["dt"] = 0.01
+    f64 = _batch(specs, 6)
+    f32 = _batch(specs, 6, precision=32)
+    worst = max(rel_err(b, a) for a, b in zip(f64, f32))
+    # float state as offsets from the initial mean: relative error ~1e-8 of max|T| (1e-6 without the offset)
+    assert worst < 1e-7, worst
