@@ -28,7 +28,10 @@ EXPORTED = ("hs2g_abi_version", "hs2g_last_error", "hs2g_create_classes", "hs2g_
             "hs2g_device_bytes", "hs2g_run_timed", "hs2g_fp64_fma_rate", "hs2g_step_static",
             "hs2g_batch_create", "hs2g_batch_destroy", "hs2g_batch_layout", "hs2g_batch_device_bytes",
             "hs2g_batch_set_temperature", "hs2g_batch_get_temperature", "hs2g_batch_set_sources",
-            "hs2g_batch_set_clock", "hs2g_batch_run", "hs2g_batch_autotune")
+            "hs2g_batch_set_clock", "hs2g_batch_run", "hs2g_batch_autotune",
+            "hs2g_adjoint_create", "hs2g_adjoint_destroy", "hs2g_adjoint_set_stream", "hs2g_adjoint_layout",
+            "hs2g_adjoint_device_bytes", "hs2g_adjoint_set_parameters", "hs2g_adjoint_forward",
+            "hs2g_adjoint_backward")
 STATIC_MAX_VOXELS = 1 << 20
 
 
@@ -60,6 +63,11 @@ class ClassProblem(ctypes.Structure):
                 ("materials", ctypes.POINTER(Material)), ("forms", ctypes.POINTER(FaceForm)),
                 ("material", ctypes.c_void_p), ("boundary_z", ctypes.c_void_p), ("boundary_y", ctypes.c_void_p),
                 ("boundary_x", ctypes.c_void_p), ("volumetric", ctypes.c_void_p)]
+
+
+class AdjointGrid(ctypes.Structure):
+    _fields_ = [("nz", ctypes.c_int64), ("ny", ctypes.c_int64), ("nx", ctypes.c_int64),
+                ("dz", ctypes.c_double), ("dy", ctypes.c_double), ("dx", ctypes.c_double)]
 
 
 class DenseProblem(ctypes.Structure):
@@ -135,6 +143,22 @@ def load():
         L.hs2g_batch_run.restype = i32
         L.hs2g_batch_autotune.argtypes = [vp, ctypes.c_char_p, i32]
         L.hs2g_batch_autotune.restype = i32
+        L.hs2g_adjoint_create.argtypes = [i32, ctypes.POINTER(AdjointGrid), dp, i32, ctypes.POINTER(vp)]
+        L.hs2g_adjoint_create.restype = i32
+        L.hs2g_adjoint_destroy.argtypes = [vp]
+        L.hs2g_adjoint_destroy.restype = None
+        L.hs2g_adjoint_set_stream.argtypes = [vp, vp]
+        L.hs2g_adjoint_set_stream.restype = i32
+        L.hs2g_adjoint_layout.argtypes = [vp, vp]
+        L.hs2g_adjoint_layout.restype = i32
+        L.hs2g_adjoint_device_bytes.argtypes = [vp]
+        L.hs2g_adjoint_device_bytes.restype = i64
+        L.hs2g_adjoint_set_parameters.argtypes = [vp, vp, vp, vp, i32]
+        L.hs2g_adjoint_set_parameters.restype = i32
+        L.hs2g_adjoint_forward.argtypes = [vp, i32, vp, vp, vp, i32, vp, vp, i32, ctypes.POINTER(dp)]
+        L.hs2g_adjoint_forward.restype = i32
+        L.hs2g_adjoint_backward.argtypes = [vp, vp, vp, vp, vp, i32, ctypes.POINTER(dp)]
+        L.hs2g_adjoint_backward.restype = i32
         L.hs2g_device_bytes.argtypes = [vp]
         L.hs2g_device_bytes.restype = i64
         if L.hs2g_abi_version() != ABI_VERSION:

@@ -1,0 +1,690 @@
+// Adjoint of the ADI timestep: gradients of a top-surface misfit with respect to per-voxel conductivity k,
+// volumetric heat capacity C = rho*c and source amplitude q, for one problem or a batch of independent
+// problems of uneven size advanced together (no counterpart in the reference, which has no derivatives).
+//
+// Model per instance (every voxel computed, exterior faces insulating, interior faces conducting with the
+// arithmetic face mean of boundary_conducting, G_f = (k_lo + k_hi) / (2 d^2)), M = C/dt, source s_n * q at
+// step n.  The step is the Douglas delta form of the forward path (hs2g_sweep.cu):
+//     r0 = L T + s_n q,  A_x y0 = r0,  A_y y1 = M y0,  A_z y2 = M y1,  T' = T + y2,   A_a = M - L_a / 2.
+// Loss per instance J = sum_n sum_{top layer k=0} (T_{n+1} - d_n)^2.
+// Discrete adjoint of one step, lambda the adjoint of T' (including the misfit gradient at T'):
+//     mu2 = A_z^-T lambda,  mu1 = A_y^-T (M mu2),  mu0 = A_x^-T (M mu1),  lambda_T = lambda + L mu0
+//     dJ/dG_f (face q|p on axis a, q the lower voxel) += -(mu0_p - mu0_q)(T_p - T_q)
+//                                                       - (mu_a,p - mu_a,q)(y_a,p - y_a,q) / 2
+//     dJ/dM_p += mu2 y1 + mu1 y0 - mu0 y0 - mu1 y1 - mu2 y2,     dJ/dq_p += s_n mu0_p
+// with (mu_a, y_a) = (mu0, y0), (mu1, y1), (mu2, y2) for a = x, y, z (L is symmetric).  The transposed
+// tridiagonal solves reuse the forward factors: A = Lo U along a line (Lo: pivots piv_r on the diagonal,
+// lo_r below; U: unit diagonal, u_r above), so A^T x = b is  w_r = b_r - u_{r-1} w_{r-1}  (rows ascending)
+// then  x_r = (w_r - lo_{r+1} x_{r+1}) / piv_r  (rows descending): the forward solve's two passes, transposed
+// and swept in the opposite direction.
+//
+// Memory: T is checkpointed every `ckpt` steps in the forward pass (ceil(nsteps/ckpt) states); the backward
+// pass recomputes a segment from its checkpoint, keeping T_n, y0, y1, y2 of each of its steps (4*ckpt states,
+// allocated by the first backward pass), then sweeps the segment backwards.
+// Concatenated layout: instance i occupies voxels [off_i, off_i + nz*ny*nx) of every field; each kernel covers
+// all instances in one launch (lines or voxels of the whole batch, the instance found by binary search).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "hs2g_internal.cuh"
+
+namespace hs2g {
+namespace {
+
+constexpr int kTh = 128;
+
+struct AInst {
+  int64_t off;              // first voxel
+  int64_t nz, ny, nx;
+  double idx2, idy2, idz2;  // 1/d^2 per axis
+  int64_t obs_off;          // first observation of the instance (nsteps * ny * nx each)
+};
+
+struct AView {
+  const AInst* inst;
+  const int64_t* vox_off;   // ninst + 1 voxel prefix
+  const int64_t* line_off;  // 3 * (ninst + 1) line prefixes, axis-major (x, y, z)
+  int ninst;
+  int64_t nvox;
+};
+
+inline unsigned nblk(int64_t n) { return (unsigned)std::max<int64_t>(1, (n + kTh - 1) / kTh); }
+
+// index of the last prefix entry <= v (prefix[0] = 0; instances are non-empty so the prefix increases)
+__device__ __forceinline__ int find_inst(const int64_t* prefix, int n, int64_t v) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(prefix + mid) <= v) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+struct Line {
+  int64_t base, stride, len;
+};
+
+// global line t of axis (0 = x, 1 = y, 2 = z) -> first voxel, stride, length
+__device__ __forceinline__ Line line_at(const AView& v, int axis, int64_t t) {
+  const int64_t* pre = v.line_off + axis * (v.ninst + 1);
+  const int i = find_inst(pre, v.ninst, t);
+  const AInst& in = v.inst[i];
+  const int64_t l = t - pre[i], nxy = in.ny * in.nx;
+  if (axis == 0) return Line{in.off + l * in.nx, 1, in.nx};
+  if (axis == 1) return Line{in.off + (l / in.nx) * nxy + l % in.nx, in.nx, in.ny};
+  return Line{in.off + l, nxy, in.nz};
+}
+
+struct Vox {
+  int64_t i, j, k, nx, ny, nz, nxy;
+  int inst;
+};
+__device__ __forceinline__ Vox vox_at(const AView& v, int64_t p) {
+  const int n = find_inst(v.vox_off, v.ninst, p);
+  const AInst& in = v.inst[n];
+  const int64_t l = p - in.off;
+  Vox r;
+  r.inst = n;
+  r.nx = in.nx; r.ny = in.ny; r.nz = in.nz; r.nxy = in.nx * in.ny;
+  r.i = l % in.nx; r.j = (l / in.nx) % in.ny; r.k = l / r.nxy;
+  return r;
+}
+
+// per-voxel low-face conductances of each axis from k (zero on the exterior), M = C / dt
+__global__ void adj_setup_kernel(AView v, const double* __restrict__ k, const double* __restrict__ C, double inv_dt,
+                                 double* __restrict__ gx, double* __restrict__ gy, double* __restrict__ gz,
+                                 double* __restrict__ M) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= v.nvox) return;
+  const Vox x = vox_at(v, p);
+  const AInst& in = v.inst[x.inst];
+  const double kp = k[p];
+  gx[p] = x.i > 0 ? 0.5 * (k[p - 1] + kp) * in.idx2 : 0.0;
+  gy[p] = x.j > 0 ? 0.5 * (k[p - x.nx] + kp) * in.idy2 : 0.0;
+  gz[p] = x.k > 0 ? 0.5 * (k[p - x.nxy] + kp) * in.idz2 : 0.0;
+  M[p] = C[p] * inv_dt;
+}
+
+// factors of A_a = M - L_a/2 per line: lo (sub-diagonal), u (normalised super-diagonal), ip (1/pivot)
+__global__ void adj_factor_kernel(AView v, int axis, int64_t nlines, const double* __restrict__ M,
+                                  const double* __restrict__ g, double* __restrict__ lo, double* __restrict__ u,
+                                  double* __restrict__ ip) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nlines) return;
+  const Line ln = line_at(v, axis, t);
+  double u_prev = 0.0;
+  for (int64_t r = 0; r < ln.len; ++r) {
+    const int64_t p = ln.base + r * ln.stride;
+    const double gl = g[p];
+    const double gh = r + 1 < ln.len ? g[p + ln.stride] : 0.0;
+    const double l = -(0.5 * gl);
+    const double piv = M[p] + 0.5 * (gl + gh) - u_prev * l;
+    const double uu = -(0.5 * gh) / piv;
+    lo[p] = l;
+    u[p] = uu;
+    ip[p] = 1.0 / piv;
+    u_prev = uu;
+  }
+}
+
+// r0 = L T + s q
+__global__ void adj_residual_kernel(AView v, const double* __restrict__ T, const double* __restrict__ gx,
+                                    const double* __restrict__ gy, const double* __restrict__ gz,
+                                    const double* __restrict__ q, double s, double* __restrict__ r0) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= v.nvox) return;
+  const Vox x = vox_at(v, p);
+  const double Tp = T[p];
+  double r = s * q[p];
+  if (x.i > 0) r += gx[p] * (T[p - 1] - Tp);
+  if (x.i + 1 < x.nx) r += gx[p + 1] * (T[p + 1] - Tp);
+  if (x.j > 0) r += gy[p] * (T[p - x.nx] - Tp);
+  if (x.j + 1 < x.ny) r += gy[p + x.nx] * (T[p + x.nx] - Tp);
+  if (x.k > 0) r += gz[p] * (T[p - x.nxy] - Tp);
+  if (x.k + 1 < x.nz) r += gz[p + x.nxy] * (T[p + x.nxy] - Tp);
+  r0[p] = r;
+}
+
+// y = A_a^-1 (scale * rhs) along each line (scale = M, or 1 when M is null); rhs may alias y (each element is
+// read before it is written).  When T_out is given, also T_out = T_in + y (T_out may alias T_in).
+__global__ void adj_solve_kernel(AView v, int axis, int64_t nlines, const double* __restrict__ M, const double* rhs,
+                                 const double* __restrict__ lo, const double* __restrict__ u,
+                                 const double* __restrict__ ip, double* y, const double* T_in, double* T_out) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nlines) return;
+  const Line ln = line_at(v, axis, t);
+  double z = 0.0;
+  for (int64_t r = 0; r < ln.len; ++r) {
+    const int64_t p = ln.base + r * ln.stride;
+    const double b = M ? M[p] * rhs[p] : rhs[p];
+    z = (b - lo[p] * z) * ip[p];
+    y[p] = z;
+  }
+  double x = 0.0;
+  for (int64_t r = ln.len - 1; r >= 0; --r) {
+    const int64_t p = ln.base + r * ln.stride;
+    x = y[p] - u[p] * x;
+    y[p] = x;
+    if (T_out) T_out[p] = T_in[p] + x;
+  }
+}
+
+// mu = A_a^-T (scale * rhs) along each line (scale = M, or 1 when M is null)
+__global__ void adj_solve_t_kernel(AView v, int axis, int64_t nlines, const double* __restrict__ M,
+                                   const double* __restrict__ rhs, const double* __restrict__ lo,
+                                   const double* __restrict__ u, const double* __restrict__ ip,
+                                   double* __restrict__ mu) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nlines) return;
+  const Line ln = line_at(v, axis, t);
+  double w = 0.0, u_prev = 0.0;
+  for (int64_t r = 0; r < ln.len; ++r) {  // U^T w = b
+    const int64_t p = ln.base + r * ln.stride;
+    const double b = M ? M[p] * rhs[p] : rhs[p];
+    w = b - u_prev * w;
+    u_prev = u[p];
+    mu[p] = w;
+  }
+  double x = 0.0, lo_next = 0.0;
+  for (int64_t r = ln.len - 1; r >= 0; --r) {  // Lo^T x = w
+    const int64_t p = ln.base + r * ln.stride;
+    x = (mu[p] - lo_next * x) * ip[p];
+    lo_next = lo[p];
+    mu[p] = x;
+  }
+}
+
+// lambda = misfit gradient of the last observation, 2 (T_N - d_{N-1}) on the top layer, 0 below
+__global__ void adj_seed_kernel(AView v, const double* __restrict__ T, const double* __restrict__ obs,
+                                int64_t obs_step, double* __restrict__ lam) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= v.nvox) return;
+  const Vox x = vox_at(v, p);
+  const AInst& in = v.inst[x.inst];
+  lam[p] = x.k == 0 ? 2.0 * (T[p] - obs[in.obs_off + obs_step * x.nxy + (p - in.off)]) : 0.0;
+}
+
+// lambda += L mu0 (+ the misfit gradient of observation obs_step, at T_n, when obs_step >= 0), and the
+// gradient accumulation of one step; one thread per voxel, each voxel owning its three low faces
+__global__ void adj_update_kernel(AView v, const double* __restrict__ gx, const double* __restrict__ gy,
+                                  const double* __restrict__ gz, const double* __restrict__ T,
+                                  const double* __restrict__ y0, const double* __restrict__ y1,
+                                  const double* __restrict__ y2, const double* __restrict__ mu0,
+                                  const double* __restrict__ mu1, const double* __restrict__ mu2, double s,
+                                  const double* __restrict__ obs, int64_t obs_step, double* __restrict__ lam,
+                                  double* __restrict__ ggx, double* __restrict__ ggy, double* __restrict__ ggz,
+                                  double* __restrict__ gM, double* __restrict__ gq) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= v.nvox) return;
+  const Vox x = vox_at(v, p);
+  const double m0 = mu0[p], Tp = T[p];
+  double lt = 0.0;
+  if (x.i > 0) lt += gx[p] * (mu0[p - 1] - m0);
+  if (x.i + 1 < x.nx) lt += gx[p + 1] * (mu0[p + 1] - m0);
+  if (x.j > 0) lt += gy[p] * (mu0[p - x.nx] - m0);
+  if (x.j + 1 < x.ny) lt += gy[p + x.nx] * (mu0[p + x.nx] - m0);
+  if (x.k > 0) lt += gz[p] * (mu0[p - x.nxy] - m0);
+  if (x.k + 1 < x.nz) lt += gz[p + x.nxy] * (mu0[p + x.nxy] - m0);
+  double l = lam[p] + lt;
+  if (obs_step >= 0 && x.k == 0) {
+    const AInst& in = v.inst[x.inst];
+    l += 2.0 * (Tp - obs[in.obs_off + obs_step * x.nxy + (p - in.off)]);
+  }
+  lam[p] = l;
+  const double m1 = mu1[p], m2 = mu2[p];
+  const double a0 = y0[p], a1 = y1[p], a2 = y2[p];
+  if (x.i > 0) {
+    const int64_t q = p - 1;
+    const double d0 = m0 - mu0[q];
+    ggx[p] += -d0 * (Tp - T[q]) - 0.5 * d0 * (a0 - y0[q]);
+  }
+  if (x.j > 0) {
+    const int64_t q = p - x.nx;
+    ggy[p] += -(m0 - mu0[q]) * (Tp - T[q]) - 0.5 * (m1 - mu1[q]) * (a1 - y1[q]);
+  }
+  if (x.k > 0) {
+    const int64_t q = p - x.nxy;
+    ggz[p] += -(m0 - mu0[q]) * (Tp - T[q]) - 0.5 * (m2 - mu2[q]) * (a2 - y2[q]);
+  }
+  gM[p] += m2 * a1 + m1 * a0 - m0 * a0 - m1 * a1 - m2 * a2;
+  gq[p] += s * m0;
+}
+
+// s + v as an unevaluated pair: returns the rounded sum, err receives its exact rounding error (Knuth's TwoSum)
+__device__ __forceinline__ double two_sum(double s, double v, double& err) {
+  const double t = s + v;
+  const double bp = t - s;
+  err = (s - (t - bp)) + (v - bp);
+  return t;
+}
+
+// misfit of step `step` per instance, as a compensated pair: part[2*(step*ninst + i)] + part[... + 1] = the sum
+// over the top layer of (T - obs)^2, accumulated with per-thread Neumaier sums and a TwoSum tree (one block of
+// 256 threads per instance, fixed order), so the loss carries no summation error that would swamp the small
+// loss differences finite-difference checks take
+__global__ void adj_misfit_kernel(AView v, const double* __restrict__ T, const double* __restrict__ obs,
+                                  int64_t step, double* __restrict__ part) {
+  __shared__ double sh_hi[256], sh_lo[256];
+  const AInst& in = v.inst[blockIdx.x];
+  const int64_t m = in.ny * in.nx;
+  const double* o = obs + in.obs_off + step * m;
+  const double* t = T + in.off;
+  double hi = 0.0, lo = 0.0;
+  for (int64_t e = threadIdx.x; e < m; e += blockDim.x) {
+    const double r = t[e] - o[e];
+    const double sq = r * r;
+    double err;
+    hi = two_sum(hi, sq, err);
+    lo += err + fma(r, r, -sq);  // the square's own rounding error, exactly
+  }
+  sh_hi[threadIdx.x] = hi;
+  sh_lo[threadIdx.x] = lo;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      double err;
+      const double s2 = two_sum(sh_hi[threadIdx.x], sh_hi[threadIdx.x + w], err);
+      sh_lo[threadIdx.x] += sh_lo[threadIdx.x + w] + err;
+      sh_hi[threadIdx.x] = s2;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const int64_t at = 2 * (step * v.ninst + blockIdx.x);
+    part[at] = sh_hi[0];
+    part[at + 1] = sh_lo[0];
+  }
+}
+
+// chain to the parameters: gk from the face gradients (G = (k_lo + k_hi) / (2 d^2)), gC = gM / dt
+__global__ void adj_chain_kernel(AView v, const double* __restrict__ ggx, const double* __restrict__ ggy,
+                                 const double* __restrict__ ggz, const double* __restrict__ gM, double inv_dt,
+                                 double* __restrict__ gk, double* __restrict__ gC) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= v.nvox) return;
+  const Vox x = vox_at(v, p);
+  const AInst& in = v.inst[x.inst];
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  if (x.i > 0) fx += ggx[p];
+  if (x.i + 1 < x.nx) fx += ggx[p + 1];
+  if (x.j > 0) fy += ggy[p];
+  if (x.j + 1 < x.ny) fy += ggy[p + x.nx];
+  if (x.k > 0) fz += ggz[p];
+  if (x.k + 1 < x.nz) fz += ggz[p + x.nxy];
+  gk[p] = 0.5 * (in.idx2 * fx + in.idy2 * fy + in.idz2 * fz);
+  gC[p] = gM[p] * inv_dt;
+}
+
+}  // namespace
+}  // namespace hs2g
+
+struct hs2g_adjoint {
+  int device = 0;
+  double dt = 0.0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = true;
+  int ninst = 0;
+  int64_t n = 0, nobs_step = 0;  // voxels; top-layer voxels of all instances (observations per step)
+  int64_t nlines[3] = {0, 0, 0};
+  std::vector<hs2g::AInst> host_inst;
+  std::vector<int64_t> host_vox_off;
+  hs2g::AInst* inst = nullptr;
+  int64_t* vox_off = nullptr;
+  int64_t* line_off = nullptr;
+  // parameters and derived fields
+  double *k = nullptr, *C = nullptr, *q = nullptr, *M = nullptr;
+  double* g[3] = {nullptr, nullptr, nullptr};
+  double *lo[3] = {nullptr, nullptr, nullptr}, *u[3] = {nullptr, nullptr, nullptr},
+         *ip[3] = {nullptr, nullptr, nullptr};
+  // run state
+  bool have_params = false;
+  int nsteps = 0, ckpt = 1;
+  std::vector<double> sched;
+  double* obs = nullptr;    // nsteps * nobs_step
+  double* ckpts = nullptr;  // ceil(nsteps / ckpt) * n
+  double* seg = nullptr;    // ckpt * 4 * n: T, y0, y1, y2 of each step of a segment
+  double* T = nullptr;      // forward state
+  double *lam = nullptr, *mu[3] = {nullptr, nullptr, nullptr};
+  double *gg[3] = {nullptr, nullptr, nullptr}, *gM = nullptr, *gq = nullptr;
+  double* parts = nullptr;  // 2 * nsteps * ninst misfit parts (compensated pairs)
+  int64_t obs_cap = 0, ckpt_cap = 0, seg_cap = 0, parts_cap = 0;
+  int64_t fixed_bytes = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+using hs2g::kTh;
+using hs2g::nblk;
+
+int afail(int code, const char* m) { return hs2g::set_last_error(code, m); }
+int acuda(cudaError_t e, const char* what) {
+  char buf[256];
+  snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+  return hs2g::set_last_error(e == cudaErrorMemoryAllocation ? HS2G_ERR_NOMEM : HS2G_ERR_CUDA, buf);
+}
+
+struct AGuard {
+  int prev = -1;
+  bool ok = false;
+  explicit AGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    ok = (prev == dev) || (cudaSetDevice(dev) == cudaSuccess);
+  }
+  ~AGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+hs2g::AView view(const hs2g_adjoint* a) { return hs2g::AView{a->inst, a->vox_off, a->line_off, a->ninst, a->n}; }
+
+cudaError_t grow(double** p, int64_t* cap, int64_t need) {
+  if (*p && *cap >= need) return cudaSuccess;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  cudaError_t e = cudaMalloc(p, sizeof(double) * std::max<int64_t>(1, need));
+  if (e == cudaSuccess) *cap = need;
+  return e;
+}
+
+// one forward step T_in -> T_out keeping y0, y1, y2 (T_out may alias T_in)
+cudaError_t fwd_step(hs2g_adjoint* a, const double* T_in, double* T_out, double* y0, double* y1, double* y2,
+                     double s) {
+  const hs2g::AView v = view(a);
+  cudaStream_t st = a->stream;
+  hs2g::adj_residual_kernel<<<nblk(a->n), kTh, 0, st>>>(v, T_in, a->g[0], a->g[1], a->g[2], a->q, s, y0);
+  hs2g::adj_solve_kernel<<<nblk(a->nlines[0]), kTh, 0, st>>>(v, 0, a->nlines[0], nullptr, y0, a->lo[0], a->u[0],
+                                                             a->ip[0], y0, nullptr, nullptr);
+  hs2g::adj_solve_kernel<<<nblk(a->nlines[1]), kTh, 0, st>>>(v, 1, a->nlines[1], a->M, y0, a->lo[1], a->u[1],
+                                                             a->ip[1], y1, nullptr, nullptr);
+  hs2g::adj_solve_kernel<<<nblk(a->nlines[2]), kTh, 0, st>>>(v, 2, a->nlines[2], a->M, y1, a->lo[2], a->u[2],
+                                                             a->ip[2], y2, T_in, T_out);
+  return cudaGetLastError();
+}
+
+// adjoint of one step: lambda (the adjoint of T_{n+1}) -> the adjoint of T_n, gradients accumulated
+cudaError_t bwd_step(hs2g_adjoint* a, const double* Tn, const double* y0, const double* y1, const double* y2,
+                     double s, int64_t obs_step) {
+  const hs2g::AView v = view(a);
+  cudaStream_t st = a->stream;
+  hs2g::adj_solve_t_kernel<<<nblk(a->nlines[2]), kTh, 0, st>>>(v, 2, a->nlines[2], nullptr, a->lam, a->lo[2],
+                                                               a->u[2], a->ip[2], a->mu[2]);
+  hs2g::adj_solve_t_kernel<<<nblk(a->nlines[1]), kTh, 0, st>>>(v, 1, a->nlines[1], a->M, a->mu[2], a->lo[1],
+                                                               a->u[1], a->ip[1], a->mu[1]);
+  hs2g::adj_solve_t_kernel<<<nblk(a->nlines[0]), kTh, 0, st>>>(v, 0, a->nlines[0], a->M, a->mu[1], a->lo[0],
+                                                               a->u[0], a->ip[0], a->mu[0]);
+  hs2g::adj_update_kernel<<<nblk(a->n), kTh, 0, st>>>(v, a->g[0], a->g[1], a->g[2], Tn, y0, y1, y2, a->mu[0],
+                                                      a->mu[1], a->mu[2], s, a->obs, obs_step, a->lam, a->gg[0],
+                                                      a->gg[1], a->gg[2], a->gM, a->gq);
+  return cudaGetLastError();
+}
+
+void adj_free(hs2g_adjoint* a) {
+  void* ptrs[] = {a->inst, a->vox_off, a->line_off, a->k, a->C, a->q, a->M, a->g[0], a->g[1], a->g[2],
+                  a->lo[0], a->lo[1], a->lo[2], a->u[0], a->u[1], a->u[2], a->ip[0], a->ip[1], a->ip[2],
+                  a->obs, a->ckpts, a->seg, a->T, a->lam, a->mu[0], a->mu[1], a->mu[2], a->gg[0], a->gg[1],
+                  a->gg[2], a->gM, a->gq, a->parts};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (a->ev0) cudaEventDestroy(a->ev0);
+  if (a->ev1) cudaEventDestroy(a->ev1);
+  if (a->stream && a->own_stream) cudaStreamDestroy(a->stream);
+}
+
+cudaMemcpyKind in_kind(int flags) { return (flags & HS2G_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice; }
+cudaMemcpyKind out_kind(int flags) { return (flags & HS2G_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost; }
+
+void read_elapsed(hs2g_adjoint* a, double* elapsed_ms) {
+  if (!elapsed_ms) return;
+  float ms = 0.f;
+  *elapsed_ms = cudaEventElapsedTime(&ms, a->ev0, a->ev1) == cudaSuccess ? ms : -1.0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hs2g_adjoint_create(int n, const hs2g_adjoint_grid* grids, double dt, int device, hs2g_adjoint** out) {
+  if (!out) return afail(HS2G_ERR_ARG, "hs2g_adjoint_create: null output");
+  *out = nullptr;
+  if (n < 1 || !grids || !(dt > 0) || !std::isfinite(dt))
+    return afail(HS2G_ERR_ARG, "hs2g_adjoint_create: bad argument");
+  std::vector<hs2g::AInst> inst((size_t)n);
+  std::vector<int64_t> vox_off((size_t)n + 1, 0), line_off(3 * ((size_t)n + 1), 0);
+  int64_t nobs = 0;
+  const int64_t limit = int64_t(1) << 40;
+  for (int i = 0; i < n; ++i) {
+    const hs2g_adjoint_grid& g = grids[i];
+    if (g.nz < 1 || g.ny < 1 || g.nx < 1 || !(g.dz > 0) || !(g.dy > 0) || !(g.dx > 0) || !std::isfinite(g.dz) ||
+        !std::isfinite(g.dy) || !std::isfinite(g.dx))
+      return afail(HS2G_ERR_ARG, "hs2g_adjoint_create: bad grid");
+    if (g.ny > limit / g.nx || g.nz > limit / (g.ny * g.nx)) return afail(HS2G_ERR_ARG, "hs2g_adjoint_create: grid too large");
+    hs2g::AInst& a = inst[i];
+    a.off = vox_off[i];
+    a.nz = g.nz;
+    a.ny = g.ny;
+    a.nx = g.nx;
+    a.idx2 = 1.0 / (g.dx * g.dx);
+    a.idy2 = 1.0 / (g.dy * g.dy);
+    a.idz2 = 1.0 / (g.dz * g.dz);
+    a.obs_off = nobs;  // in units of nsteps, scaled when the step count is known
+    nobs += g.ny * g.nx;
+    vox_off[i + 1] = vox_off[i] + g.nz * g.ny * g.nx;
+    if (vox_off[i + 1] > limit) return afail(HS2G_ERR_ARG, "hs2g_adjoint_create: batch too large");
+    line_off[0 * (n + 1) + i + 1] = line_off[0 * (n + 1) + i] + g.nz * g.ny;
+    line_off[1 * (n + 1) + i + 1] = line_off[1 * (n + 1) + i] + g.nz * g.nx;
+    line_off[2 * (n + 1) + i + 1] = line_off[2 * (n + 1) + i] + g.ny * g.nx;
+  }
+  AGuard guard(device);
+  if (!guard.ok) return afail(HS2G_ERR_CUDA, "hs2g_adjoint_create: cannot select device");
+  hs2g_adjoint* a = new hs2g_adjoint();
+  a->device = device;
+  a->dt = dt;
+  a->ninst = n;
+  a->n = vox_off[n];
+  a->nobs_step = nobs;
+  for (int ax = 0; ax < 3; ++ax) a->nlines[ax] = line_off[ax * (n + 1) + n];
+  a->host_inst = inst;
+  a->host_vox_off = vox_off;
+  cudaError_t e = cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&a->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&a->ev1);
+  if (e == cudaSuccess) e = cudaMalloc(&a->inst, sizeof(hs2g::AInst) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&a->vox_off, sizeof(int64_t) * (n + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&a->line_off, sizeof(int64_t) * 3 * (n + 1));
+  double** per_voxel[] = {&a->k, &a->C, &a->q, &a->M, &a->g[0], &a->g[1], &a->g[2], &a->lo[0], &a->lo[1],
+                          &a->lo[2], &a->u[0], &a->u[1], &a->u[2], &a->ip[0], &a->ip[1], &a->ip[2], &a->T,
+                          &a->lam, &a->mu[0], &a->mu[1], &a->mu[2], &a->gg[0], &a->gg[1], &a->gg[2], &a->gM,
+                          &a->gq};
+  const int nfields = (int)(sizeof(per_voxel) / sizeof(per_voxel[0]));
+  for (double** p : per_voxel)
+    if (e == cudaSuccess) e = cudaMalloc(p, sizeof(double) * a->n);
+  if (e == cudaSuccess) e = cudaMemcpy(a->inst, inst.data(), sizeof(hs2g::AInst) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(a->vox_off, vox_off.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(a->line_off, line_off.data(), sizeof(int64_t) * 3 * (n + 1), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    const int rc = acuda(e, "hs2g_adjoint_create");
+    adj_free(a);
+    delete a;
+    return rc;
+  }
+  a->fixed_bytes = (int64_t)nfields * a->n * (int64_t)sizeof(double);
+  *out = a;
+  return HS2G_OK;
+}
+
+void hs2g_adjoint_destroy(hs2g_adjoint* a) {
+  if (!a) return;
+  AGuard guard(a->device);
+  cudaStreamSynchronize(a->stream);
+  adj_free(a);
+  delete a;
+}
+
+int hs2g_adjoint_set_stream(hs2g_adjoint* a, void* stream) {
+  if (!a) return afail(HS2G_ERR_ARG, "null handle");
+  if (!a->own_stream && a->stream == (cudaStream_t)stream) return HS2G_OK;
+  AGuard guard(a->device);
+  cudaStreamSynchronize(a->stream);
+  if (a->own_stream) cudaStreamDestroy(a->stream);
+  a->stream = (cudaStream_t)stream;  // NULL = the legacy default stream
+  a->own_stream = false;
+  return HS2G_OK;
+}
+
+int hs2g_adjoint_layout(const hs2g_adjoint* a, int64_t* offsets) {
+  if (!a || !offsets) return afail(HS2G_ERR_ARG, "null argument");
+  for (int i = 0; i <= a->ninst; ++i) offsets[i] = a->host_vox_off[i];
+  return HS2G_OK;
+}
+
+int64_t hs2g_adjoint_device_bytes(const hs2g_adjoint* a) {
+  if (!a) return 0;
+  return a->fixed_bytes + (int64_t)sizeof(double) * (a->obs_cap + a->ckpt_cap + a->seg_cap + a->parts_cap);
+}
+
+int hs2g_adjoint_set_parameters(hs2g_adjoint* a, const double* k, const double* C, const double* q, int flags) {
+  if (!a || !k || !C || !q) return afail(HS2G_ERR_ARG, "hs2g_adjoint_set_parameters: null argument");
+  AGuard guard(a->device);
+  cudaStream_t st = a->stream;
+  const int64_t n = a->n;
+  const cudaMemcpyKind kind = in_kind(flags);
+  a->have_params = false;
+  a->nsteps = 0;
+  cudaError_t e = cudaMemcpyAsync(a->k, k, sizeof(double) * n, kind, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(a->C, C, sizeof(double) * n, kind, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(a->q, q, sizeof(double) * n, kind, st);
+  if (e != cudaSuccess) return acuda(e, "hs2g_adjoint_set_parameters");
+  const hs2g::AView v = view(a);
+  hs2g::adj_setup_kernel<<<nblk(n), kTh, 0, st>>>(v, a->k, a->C, 1.0 / a->dt, a->g[0], a->g[1], a->g[2], a->M);
+  for (int ax = 0; ax < 3; ++ax)
+    hs2g::adj_factor_kernel<<<nblk(a->nlines[ax]), kTh, 0, st>>>(v, ax, a->nlines[ax], a->M, a->g[ax], a->lo[ax],
+                                                                a->u[ax], a->ip[ax]);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return acuda(e, "hs2g_adjoint_set_parameters");
+  a->have_params = true;
+  return HS2G_OK;
+}
+
+int hs2g_adjoint_forward(hs2g_adjoint* a, int nsteps, const double* schedule, const double* T0, const double* obs,
+                         int ckpt, double* loss, double* T_out, int flags, double* elapsed_ms) {
+  if (!a || nsteps < 1 || !schedule || !T0 || !obs || ckpt < 1 || !loss)
+    return afail(HS2G_ERR_ARG, "hs2g_adjoint_forward: bad argument");
+  if (!a->have_params) return afail(HS2G_ERR_STATE, "hs2g_adjoint_forward: parameters not set");
+  for (int s = 0; s < nsteps; ++s)
+    if (!std::isfinite(schedule[s])) return afail(HS2G_ERR_ARG, "hs2g_adjoint_forward: non-finite schedule");
+  AGuard guard(a->device);
+  cudaStream_t st = a->stream;
+  const int64_t n = a->n;
+  ckpt = std::min(ckpt, nsteps);
+  const int64_t nck = (nsteps + ckpt - 1) / ckpt;
+  a->nsteps = 0;
+  cudaError_t e = cudaStreamSynchronize(st);  // buffers may be reallocated below
+  if (e == cudaSuccess) e = grow(&a->obs, &a->obs_cap, (int64_t)nsteps * a->nobs_step);
+  if (e == cudaSuccess) e = grow(&a->ckpts, &a->ckpt_cap, nck * n);
+  if (e == cudaSuccess) e = grow(&a->parts, &a->parts_cap, (int64_t)2 * nsteps * a->ninst);
+  if (e != cudaSuccess) return acuda(e, "hs2g_adjoint_forward: device allocation");
+  std::vector<hs2g::AInst> inst = a->host_inst;
+  for (auto& in : inst) in.obs_off *= nsteps;
+  e = cudaMemcpyAsync(a->inst, inst.data(), sizeof(hs2g::AInst) * a->ninst, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(a->obs, obs, sizeof(double) * nsteps * a->nobs_step, in_kind(flags), st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(a->T, T0, sizeof(double) * n, in_kind(flags), st);
+  if (e == cudaSuccess) e = cudaEventRecord(a->ev0, st);
+  a->sched.assign(schedule, schedule + nsteps);
+  const hs2g::AView v = view(a);
+  for (int s = 0; s < nsteps && e == cudaSuccess; ++s) {
+    if (s % ckpt == 0)
+      e = cudaMemcpyAsync(a->ckpts + (int64_t)(s / ckpt) * n, a->T, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                          st);
+    // the adjoint buffers are free during the forward pass and hold the increments
+    if (e == cudaSuccess) e = fwd_step(a, a->T, a->T, a->mu[0], a->mu[1], a->mu[2], a->sched[s]);
+    if (e == cudaSuccess) {
+      hs2g::adj_misfit_kernel<<<a->ninst, 256, 0, st>>>(v, a->T, a->obs, s, a->parts);
+      e = cudaGetLastError();
+    }
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(a->ev1, st);
+  std::vector<double> parts((size_t)2 * nsteps * a->ninst);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(parts.data(), a->parts, sizeof(double) * parts.size(), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && T_out) e = cudaMemcpyAsync(T_out, a->T, sizeof(double) * n, out_kind(flags), st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return acuda(e, "hs2g_adjoint_forward");
+  read_elapsed(a, elapsed_ms);
+  for (int i = 0; i < a->ninst; ++i) {  // Neumaier sum of the per-step pairs
+    double acc = 0.0, comp = 0.0;
+    for (int s = 0; s < nsteps; ++s)
+      for (int h = 0; h < 2; ++h) {
+        const double v = parts[2 * ((size_t)s * a->ninst + i) + h];
+        const double t = acc + v;
+        comp += std::fabs(acc) >= std::fabs(v) ? (acc - t) + v : (v - t) + acc;
+        acc = t;
+      }
+    loss[i] = acc + comp;
+  }
+  a->nsteps = nsteps;
+  a->ckpt = ckpt;
+  return HS2G_OK;
+}
+
+int hs2g_adjoint_backward(hs2g_adjoint* a, double* gk, double* gC, double* gq, double* gT0, int flags,
+                          double* elapsed_ms) {
+  if (!a || !gk || !gC || !gq) return afail(HS2G_ERR_ARG, "hs2g_adjoint_backward: null argument");
+  if (a->nsteps < 1) return afail(HS2G_ERR_STATE, "hs2g_adjoint_backward: no forward pass to differentiate");
+  AGuard guard(a->device);
+  cudaStream_t st = a->stream;
+  const hs2g::AView v = view(a);
+  const int64_t n = a->n;
+  const int N = a->nsteps, C = a->ckpt;
+  // the segment store (T, y0, y1, y2 of ckpt steps) exists only while gradients are taken
+  cudaError_t e = grow(&a->seg, &a->seg_cap, (int64_t)C * 4 * n);
+  if (e != cudaSuccess) return acuda(e, "hs2g_adjoint_backward: device allocation");
+  e = cudaEventRecord(a->ev0, st);
+  double* zero_list[] = {a->gg[0], a->gg[1], a->gg[2], a->gM, a->gq};
+  for (double* p : zero_list)
+    if (e == cudaSuccess) e = cudaMemsetAsync(p, 0, sizeof(double) * n, st);
+  if (e == cudaSuccess) {
+    hs2g::adj_seed_kernel<<<nblk(n), kTh, 0, st>>>(v, a->T, a->obs, N - 1, a->lam);
+    e = cudaGetLastError();
+  }
+  const int nseg = (N + C - 1) / C;
+  for (int sg = nseg - 1; sg >= 0 && e == cudaSuccess; --sg) {
+    const int s0 = sg * C, s1 = std::min(N, s0 + C);
+    // recompute the segment: slot j holds T, y0, y1, y2 of step s0 + j; the end state is not needed
+    e = cudaMemcpyAsync(a->seg, a->ckpts + (int64_t)sg * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, st);
+    for (int s = s0; s < s1 && e == cudaSuccess; ++s) {
+      double* slot = a->seg + (int64_t)(s - s0) * 4 * n;
+      double* next = s + 1 < s1 ? slot + 4 * n : a->mu[0];
+      e = fwd_step(a, slot, next, slot + n, slot + 2 * n, slot + 3 * n, a->sched[s]);
+    }
+    for (int s = s1 - 1; s >= s0 && e == cudaSuccess; --s) {
+      const double* slot = a->seg + (int64_t)(s - s0) * 4 * n;
+      // T_s (s >= 1) is the state observed after step s - 1
+      e = bwd_step(a, slot, slot + n, slot + 2 * n, slot + 3 * n, a->sched[s], s >= 1 ? s - 1 : -1);
+    }
+  }
+  if (e == cudaSuccess) {
+    hs2g::adj_chain_kernel<<<nblk(n), kTh, 0, st>>>(v, a->gg[0], a->gg[1], a->gg[2], a->gM, 1.0 / a->dt, a->mu[0],
+                                                    a->mu[1]);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(a->ev1, st);
+  const cudaMemcpyKind kind = out_kind(flags);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(gk, a->mu[0], sizeof(double) * n, kind, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(gC, a->mu[1], sizeof(double) * n, kind, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(gq, a->gq, sizeof(double) * n, kind, st);
+  if (e == cudaSuccess && gT0) e = cudaMemcpyAsync(gT0, a->lam, sizeof(double) * n, kind, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return acuda(e, "hs2g_adjoint_backward");
+  read_elapsed(a, elapsed_ms);
+  return HS2G_OK;
+}
+
+}  // extern "C"

@@ -333,3 +333,78 @@ def sources_small(seed=9, nz=6, ny=5, nx=4, dt=0.01, nsteps=5):
                        ["zdecay", 0.02, [1.0, 0.0, 0.0], 0.0005, "zgrid", 1e-3, 1e4, 0.0007]],
         "arrays": dict(a, zgrid=zgrid, pj=pj),
     }
+
+
+# ----------------------------------------------------------------------------------------------------------
+# adjoint (inverse-problem) workloads: per-voxel parameters, top-surface observations
+# ----------------------------------------------------------------------------------------------------------
+def flash_observations(rng, shape, nsteps, dt, d, k, C, q_top, T0=T_AMBIENT, noise=0.01):
+    """Seeded synthetic top-surface temperatures (nsteps, ny, nx): the semi-infinite-body response to a flash
+    of q_top W/m^3 absorbed in a top layer of depth d during the first step, T0 + E / (e sqrt(pi t)) with
+    E = q_top d dt (J/m^2) and effusivity e = sqrt(k C), plus Gaussian noise of `noise` K."""
+    nz, ny, nx = shape
+    t = dt * (np.arange(nsteps) + 1.0)
+    rise = q_top * d * dt / (np.sqrt(k * C) * np.sqrt(np.pi * t))
+    obs = T0 + rise[:, None, None] + noise * rng.standard_normal((nsteps, ny, nx))
+    return obs
+
+
+def adjoint_steel(seed=3, nz=32, ny=128, nx=128, d=1e-3, dt=0.01, nsteps=500, ckpt=50, sigma=0.2,
+                  power=1e9):
+    """Single-instance adjoint workload: (32,128,128) steel at 1 mm, per-voxel k lognormal around 54 W/m/K
+    (sigma 0.2), rho*c = 7850*470, flash ``power`` W/m^3 in the top layer during the first 10 ms step, T0 = 293 K,
+    500 steps of 10 ms, checkpoint every 50; observations of the top surface seeded-synthetic."""
+    rng = np.random.default_rng(seed)
+    shape = (nz, ny, nx)
+    k = 54.0 * np.exp(sigma * rng.standard_normal(shape) - 0.5 * sigma * sigma)
+    C = np.full(shape, 7850.0 * 470.0)
+    q = np.zeros(shape)
+    q[0] = power
+    schedule = np.zeros(nsteps)
+    schedule[0] = 1.0
+    obs = flash_observations(rng, shape, nsteps, dt, d, 54.0, 7850.0 * 470.0, power)
+    return {"name": "adjoint_steel", "shape": shape, "spacing": (d, d, d), "dt": dt, "nsteps": nsteps,
+            "ckpt": ckpt, "k": k, "C": C, "q": q, "T0": np.full(shape, T_AMBIENT), "schedule": schedule,
+            "obs": obs}
+
+
+def two_phase_k(rng, shape, matrix=5.0, inclusion=0.3, fraction=0.1, radius_range=(1, 4)):
+    """Matrix conductivity with seeded box inclusions (half-widths in radius_range) of `inclusion` W/m/K, added
+    sixteen at a time until they cover at least `fraction` of the voxels."""
+    nz, ny, nx = shape
+    k = np.full(shape, matrix)
+    mask = np.zeros(shape, dtype=bool)
+    target = fraction * mask.size
+    while mask.sum() < target:
+        for _ in range(16):
+            r = rng.integers(radius_range[0], radius_range[1] + 1, size=3)
+            c = [int(rng.integers(0, n)) for n in shape]
+            sl = tuple(slice(max(0, c[a] - r[a]), min(shape[a], c[a] + r[a] + 1)) for a in range(3))
+            mask[sl] = True
+    k[mask] = inclusion
+    return k
+
+
+def adjoint_batch(seed=4, n=32, nz_range=(24, 48), nxy_range=(96, 192), d=0.5e-3, dt=0.005, nsteps=400,
+                  ckpt=40, power=2e9):
+    """Batched adjoint workload: ``n`` instances, nz uniform in nz_range and ny,nx in nxy_range, per-voxel k a
+    two-phase field (matrix 5 W/m/K, inclusions 0.3 W/m/K at 10% volume fraction), rho*c = 1550*1100, flash
+    ``power`` W/m^3 in the top layer during the first 5 ms step, 400 steps, checkpoint every 40."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for c in range(n):
+        nz = int(rng.integers(nz_range[0], nz_range[1] + 1))
+        ny = int(rng.integers(nxy_range[0], nxy_range[1] + 1))
+        nx = int(rng.integers(nxy_range[0], nxy_range[1] + 1))
+        shape = (nz, ny, nx)
+        k = two_phase_k(rng, shape)
+        Cv = 1550.0 * 1100.0
+        q = np.zeros(shape)
+        q[0] = power
+        schedule = np.zeros(nsteps)
+        schedule[0] = 1.0
+        obs = flash_observations(rng, shape, nsteps, dt, d, 5.0, Cv, power)
+        out.append({"name": "adjoint_batch_%d" % c, "shape": shape, "spacing": (d, d, d), "dt": dt,
+                    "nsteps": nsteps, "ckpt": ckpt, "k": k, "C": np.full(shape, Cv), "q": q,
+                    "T0": np.full(shape, T_AMBIENT), "schedule": schedule, "obs": obs})
+    return out

@@ -219,6 +219,41 @@ int hs2g_batch_run(hs2g_batch* b, int nsteps, int flags, double* elapsed_ms);
 /* Time candidate launch shapes per axis on this batch and keep the fastest; writes a report. */
 int hs2g_batch_autotune(hs2g_batch* b, char* report, int report_len);
 
+/*
+ * Adjoint (no counterpart in the reference, which has no derivatives): gradients of a top-surface misfit
+ *     J_i = sum_{n < nsteps} sum_{y,x} (T_{n+1}[0, y, x] - obs_i[n, y, x])^2
+ * with respect to per-voxel conductivity k (W/m/K), volumetric heat capacity C = rho*c (J/m^3/K), source
+ * amplitude q (W/m^3, applied at step n as schedule[n] * q) and the initial temperature, for n instances of
+ * uneven size in one concatenated state (a single problem is n = 1).  Each instance is a fully computed box,
+ * insulating outside, its interior faces conducting with the arithmetic face mean of boundary_conducting
+ * (boundary_conducting.py:7-71); the step is the same Douglas delta form as hs2g_step.  k must be >= 0 and
+ * C > 0.  The forward pass checkpoints T every `ckpt` steps; the backward pass recomputes one segment at a
+ * time from its checkpoint and runs the transposed tridiagonal solves in reverse order (z, y, x).  Every
+ * kernel of a sweep covers all instances in one launch.
+ */
+typedef struct {
+  int64_t nz, ny, nx;
+  double dz, dy, dx;                /* m */
+} hs2g_adjoint_grid;
+typedef struct hs2g_adjoint hs2g_adjoint;
+int hs2g_adjoint_create(int n, const hs2g_adjoint_grid* grids, double dt, int device, hs2g_adjoint** out);
+void hs2g_adjoint_destroy(hs2g_adjoint* a);
+/* Queue work on a caller's cudaStream_t (NULL = legacy default stream) instead of the handle's own stream. */
+int hs2g_adjoint_set_stream(hs2g_adjoint* a, void* stream);
+/* offsets[n+1]: instance i's (nz, ny, nx) fields start at voxel offsets[i] of every concatenated array. */
+int hs2g_adjoint_layout(const hs2g_adjoint* a, int64_t* offsets);
+int64_t hs2g_adjoint_device_bytes(const hs2g_adjoint* a);
+/* k, C, q: offsets[n] doubles each, host or device (HS2G_DEVICE); compiles conductances and line factors. */
+int hs2g_adjoint_set_parameters(hs2g_adjoint* a, const double* k, const double* C, const double* q, int flags);
+/* T0: offsets[n] doubles; obs: per instance in order, nsteps * ny_i * nx_i doubles (host or device, flags);
+   schedule[nsteps] host.  loss[n] receives J_i; T_out (offsets[n] doubles, or NULL) the final temperature;
+   elapsed_ms (or NULL) the device time of the steps. */
+int hs2g_adjoint_forward(hs2g_adjoint* a, int nsteps, const double* schedule, const double* T0, const double* obs,
+                         int ckpt, double* loss, double* T_out, int flags, double* elapsed_ms);
+/* dJ_i/dk, dJ_i/dC, dJ_i/dq and (gT0 not NULL) dJ_i/dT0 of the last forward pass, offsets[n] doubles each. */
+int hs2g_adjoint_backward(hs2g_adjoint* a, double* gk, double* gC, double* gq, double* gT0, int flags,
+                          double* elapsed_ms);
+
 /* Copy the compiled face conductances and capacities to host buffers (any may be NULL). */
 int hs2g_get_faces(hs2g_handle* h, double* Gz, double* Gy, double* Gx, double* capacity, uint8_t* fixed);
 

@@ -1,0 +1,165 @@
+"""A numpy model of libhs2g's adjoint kernels (hs2g_adjoint.cu), operation for operation (test helper, CPU).
+
+It repeats the forward step in the LU form the device uses (per-line factors lo, u, 1/pivot), the
+checkpointed forward pass, the segment-by-segment recompute and the reverse sweep -- transposed solves in the
+order z, y, x, then lambda += L mu0, the face / capacity / source gradient accumulation and the chain to k
+and C -- so the adjoint's derivation and its checkpoint bookkeeping can be checked against autograd through
+``torch_adi`` on machines without a GPU.  It is never used by the product.
+"""
+import numpy as np
+
+
+def low_faces(k, spacing):
+    """Per-voxel low-face conductances of each axis (zero on the exterior), as adj_setup_kernel."""
+    dz, dy, dx = spacing
+    gz = np.zeros_like(k)
+    gy = np.zeros_like(k)
+    gx = np.zeros_like(k)
+    gz[1:] = 0.5 * (k[:-1] + k[1:]) * (1.0 / (dz * dz))
+    gy[:, 1:] = 0.5 * (k[:, :-1] + k[:, 1:]) * (1.0 / (dy * dy))
+    gx[:, :, 1:] = 0.5 * (k[:, :, :-1] + k[:, :, 1:]) * (1.0 / (dx * dx))
+    return gz, gy, gx
+
+
+def factor(M, g, axis):
+    """(lo, u, ip) of M - L_axis/2 along `axis`, as adj_factor_kernel."""
+    Mt = np.moveaxis(M, axis, -1)
+    gt = np.moveaxis(g, axis, -1)
+    n = Mt.shape[-1]
+    lo = np.zeros_like(Mt)
+    u = np.zeros_like(Mt)
+    ip = np.zeros_like(Mt)
+    u_prev = np.zeros(Mt.shape[:-1])
+    for r in range(n):
+        gl = gt[..., r]
+        gh = gt[..., r + 1] if r + 1 < n else np.zeros_like(gl)
+        l = -(0.5 * gl)
+        piv = Mt[..., r] + 0.5 * (gl + gh) - u_prev * l
+        uu = -(0.5 * gh) / piv
+        lo[..., r] = l
+        u[..., r] = uu
+        ip[..., r] = 1.0 / piv
+        u_prev = uu
+    return tuple(np.moveaxis(a, -1, axis) for a in (lo, u, ip))
+
+
+def solve(f, b, axis):
+    lo, u, ip = (np.moveaxis(a, axis, -1) for a in f)
+    bt = np.moveaxis(b, axis, -1)
+    n = bt.shape[-1]
+    y = np.zeros_like(bt)
+    z = np.zeros(bt.shape[:-1])
+    for r in range(n):
+        z = (bt[..., r] - lo[..., r] * z) * ip[..., r]
+        y[..., r] = z
+    x = np.zeros(bt.shape[:-1])
+    for r in range(n - 1, -1, -1):
+        x = y[..., r] - u[..., r] * x
+        y[..., r] = x
+    return np.moveaxis(y, -1, axis)
+
+
+def solve_t(f, b, axis):
+    lo, u, ip = (np.moveaxis(a, axis, -1) for a in f)
+    bt = np.moveaxis(b, axis, -1)
+    n = bt.shape[-1]
+    mu = np.zeros_like(bt)
+    w = np.zeros(bt.shape[:-1])
+    u_prev = np.zeros(bt.shape[:-1])
+    for r in range(n):
+        w = bt[..., r] - u_prev * w
+        u_prev = u[..., r]
+        mu[..., r] = w
+    x = np.zeros(bt.shape[:-1])
+    lo_next = np.zeros(bt.shape[:-1])
+    for r in range(n - 1, -1, -1):
+        x = (mu[..., r] - lo_next * x) * ip[..., r]
+        lo_next = lo[..., r]
+        mu[..., r] = x
+    return np.moveaxis(mu, -1, axis)
+
+
+def lap(T, gz, gy, gx):
+    """(L T)_p = sum over the six faces of G (T_neighbour - T_p), low-face arrays."""
+    out = np.zeros_like(T)
+    out[:, :, 1:] += gx[:, :, 1:] * (T[:, :, :-1] - T[:, :, 1:])
+    out[:, :, :-1] += gx[:, :, 1:] * (T[:, :, 1:] - T[:, :, :-1])
+    out[:, 1:] += gy[:, 1:] * (T[:, :-1] - T[:, 1:])
+    out[:, :-1] += gy[:, 1:] * (T[:, 1:] - T[:, :-1])
+    out[1:] += gz[1:] * (T[:-1] - T[1:])
+    out[:-1] += gz[1:] * (T[1:] - T[:-1])
+    return out
+
+
+class Model(object):
+    def __init__(self, k, C, q, dt, spacing):
+        self.k, self.C, self.q, self.dt, self.spacing = k, C, q, dt, spacing
+        self.g = low_faces(k, spacing)
+        self.M = C * (1.0 / dt)
+        gz, gy, gx = self.g
+        self.f = [factor(self.M, gx, 2), factor(self.M, gy, 1), factor(self.M, gz, 0)]
+
+    def fwd_step(self, T, s):
+        gz, gy, gx = self.g
+        y0 = solve(self.f[0], lap(T, gz, gy, gx) + s * self.q, 2)
+        y1 = solve(self.f[1], self.M * y0, 1)
+        y2 = solve(self.f[2], self.M * y1, 0)
+        return T + y2, y0, y1, y2
+
+    def forward(self, T0, schedule, obs, ckpt):
+        self.schedule, self.obs, self.ckpt = list(schedule), obs, min(ckpt, len(schedule))
+        self.ckpts = []
+        T = T0.copy()
+        J = 0.0
+        for s, sv in enumerate(self.schedule):
+            if s % self.ckpt == 0:
+                self.ckpts.append(T.copy())
+            T = self.fwd_step(T, sv)[0]
+            J += float(((T[0] - obs[s]) ** 2).sum())
+        self.T_end = T
+        return J
+
+    def backward(self):
+        gz, gy, gx = self.g
+        N, Cp = len(self.schedule), self.ckpt
+        gg = [np.zeros_like(self.k) for _ in range(3)]       # x, y, z low-face gradients
+        gM = np.zeros_like(self.k)
+        gq = np.zeros_like(self.k)
+        lam = np.zeros_like(self.k)
+        lam[0] = 2.0 * (self.T_end[0] - self.obs[N - 1])
+        for sg in range((N + Cp - 1) // Cp - 1, -1, -1):
+            s0, s1 = sg * Cp, min(N, sg * Cp + Cp)
+            slots = []
+            T = self.ckpts[sg]
+            for s in range(s0, s1):
+                Tn, y0, y1, y2 = self.fwd_step(T, self.schedule[s])
+                slots.append((T, y0, y1, y2))
+                T = Tn
+            for s in range(s1 - 1, s0 - 1, -1):
+                Tn, y0, y1, y2 = slots[s - s0]
+                mu2 = solve_t(self.f[2], lam, 0)
+                mu1 = solve_t(self.f[1], self.M * mu2, 1)
+                mu0 = solve_t(self.f[0], self.M * mu1, 2)
+                lam = lam + lap(mu0, gz, gy, gx)
+                if s >= 1:
+                    lam[0] += 2.0 * (Tn[0] - self.obs[s - 1])
+                d0 = mu0[:, :, 1:] - mu0[:, :, :-1]
+                gg[0][:, :, 1:] += -d0 * (Tn[:, :, 1:] - Tn[:, :, :-1]) - 0.5 * d0 * (y0[:, :, 1:] - y0[:, :, :-1])
+                gg[1][:, 1:] += (-(mu0[:, 1:] - mu0[:, :-1]) * (Tn[:, 1:] - Tn[:, :-1])
+                                 - 0.5 * (mu1[:, 1:] - mu1[:, :-1]) * (y1[:, 1:] - y1[:, :-1]))
+                gg[2][1:] += (-(mu0[1:] - mu0[:-1]) * (Tn[1:] - Tn[:-1])
+                              - 0.5 * (mu2[1:] - mu2[:-1]) * (y2[1:] - y2[:-1]))
+                gM += mu2 * y1 + mu1 * y0 - mu0 * y0 - mu1 * y1 - mu2 * y2
+                gq += self.schedule[s] * mu0
+        dz, dy, dx = self.spacing
+        gk = np.zeros_like(self.k)
+        for a, (gf, d) in enumerate(zip(gg, (dx, dy, dz))):
+            ax = 2 - a
+            sl_hi = [slice(None)] * 3
+            sl_lo = [slice(None)] * 3
+            sl_hi[ax] = slice(1, None)
+            sl_lo[ax] = slice(None, -1)
+            face = gf[tuple(sl_hi)] * (0.5 / (d * d))
+            gk[tuple(sl_hi)] += face
+            gk[tuple(sl_lo)] += face
+        return gk, gM / self.dt, gq, lam
