@@ -13,7 +13,10 @@ Prints one JSON line.  ``value`` counts computed voxels (64*512*512) per second 
 HBM; ``e2e`` is the same metric through the C ABI with host buffers (host->device copy of T, the step,
 device->host copy of T, every step); ``roofline`` is the dominant sweep kernel against the measured HBM copy
 bandwidth; ``fp64_roofline`` the whole step against the measured FP64 FMA rate, the resource that binds;
-``cpu_baseline`` the reference (or, where it cannot be built, the oracle) on the host cores.
+``cpu_baseline`` the reference (or, where it cannot be built, the oracle) on the host cores.  ``batched`` is
+the 256-instance uneven batch (FP64 and FP32) against a per-instance loop of the plain path; ``adjoint`` the
+gradient evaluations per second of the (32,128,128) steel inverse problem and of the 32-instance batched
+adjoint against a loop of single-instance adjoints.
 """
 import argparse
 import json
@@ -55,6 +58,9 @@ def parse_args():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-instances", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=100)
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-loop", type=int, default=32,
+                    help="instances of the batched adjoint workload timed as a loop of single-instance adjoints")
     ap.add_argument("--cpu-worker", default=None, help=argparse.SUPPRESS)
     return ap.parse_args()
 
@@ -342,6 +348,75 @@ def batched_measurement(args, world, rank, dev):
     return out
 
 
+def adjoint_measurement(args, world, rank, dev):
+    """Gradient evaluations (forward pass + checkpointed backward pass) per second.
+
+    steel: one (32,128,128) steel instance, per-voxel lognormal k, 500 steps of 10 ms, checkpoint every 50.
+    batched: 32 uneven two-phase instances (nz 24..48, ny,nx 96..192), 400 steps of 5 ms, checkpoint every 40,
+    all in one concatenated state (one launch per sweep over every instance), against a loop of the
+    single-instance adjoint over the same instances.  Device time from CUDA events around the steps."""
+    import numpy as np
+    import torch
+    from heatsim2_gb300 import workloads as W
+    from heatsim2_gb300.adjoint import Adjoint
+    from heatsim2_gb300.batch import shard
+
+    out = {}
+    w = W.adjoint_steel()
+    a = Adjoint([(w["shape"], w["spacing"])], w["dt"])
+    a.set_parameters(w["k"], w["C"], w["q"])
+    for _ in range(2):  # warm-up, then the timed evaluation
+        a.forward(w["T0"], w["obs"], w["schedule"], w["ckpt"])
+        a.backward()
+    fwd, bwd = a.forward_ms, a.backward_ms
+    vox = int(np.prod(w["shape"]))
+    out["steel"] = {"workload": "steel (32,128,128) lognormal k, 500 steps dt=10 ms, checkpoint 50",
+                    "gradient_evals_per_s": 1e3 / (fwd + bwd), "forward_ms": fwd, "backward_ms": bwd,
+                    "forward_voxel_steps_per_s": vox * w["nsteps"] / (fwd * 1e-3),
+                    "device_bytes": a.device_bytes}
+    del a
+    insts_all = W.adjoint_batch()
+    sizes = [int(np.prod(x["shape"])) for x in insts_all]
+    insts = [insts_all[i] for i in shard(sizes, world, rank)]
+    b = Adjoint([(x["shape"], x["spacing"]) for x in insts], insts[0]["dt"])
+    b.set_parameters([x["k"] for x in insts], [x["C"] for x in insts], [x["q"] for x in insts])
+    args_f = ([x["T0"] for x in insts], [x["obs"] for x in insts], insts[0]["schedule"], insts[0]["ckpt"])
+    for _ in range(2):
+        b.forward(*args_f)
+        gb = b.backward()
+    batch_ms = b.forward_ms + b.backward_ms
+    bytes_b = b.device_bytes
+    del b
+    torch.cuda.empty_cache()
+    loop_ms, worst = 0.0, 0.0
+    nloop = min(args.adjoint_loop, len(insts))
+    for i, x in enumerate(insts[:nloop]):
+        s = Adjoint([(x["shape"], x["spacing"])], x["dt"])
+        s.set_parameters(x["k"], x["C"], x["q"])
+        s.forward(x["T0"], x["obs"], x["schedule"], x["ckpt"])
+        g = s.backward()
+        loop_ms += s.forward_ms + s.backward_ms
+        worst = max(worst, max(float(np.abs(u - v[i]).max() / max(np.abs(v[i]).max(), 1e-300))
+                               for u, v in zip(g, gb)))
+        del s
+    loop_ms *= len(insts) / nloop
+    batch_evals = len(insts) / (batch_ms * 1e-3)
+    loop_evals = len(insts) / (loop_ms * 1e-3)
+    if world > 1:
+        t = torch.tensor([batch_ms, loop_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        batch_evals = len(insts_all) / (float(t[0]) * 1e-3)
+        loop_evals = len(insts_all) / (float(t[1]) * 1e-3)
+    out["batched"] = {"workload": "%d uneven two-phase instances (nz 24..48, ny,nx 96..192), 400 steps dt=5 ms, "
+                                  "checkpoint 40" % len(insts_all),
+                      "voxels": sum(sizes), "gradient_evals_per_s": batch_evals, "ms_per_eval_batch": batch_ms,
+                      "device_bytes": bytes_b,
+                      "single_loop": {"gradient_evals_per_s": loop_evals, "instances_timed": nloop,
+                                      "max_rel_diff_vs_batch": worst},
+                      "speedup_vs_loop": batch_evals / loop_evals}
+    return out
+
+
 # ------------------------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------------------------
@@ -446,6 +521,10 @@ def gpu_arm(args, world, rank, local_rank):
         del P, S
         torch.cuda.empty_cache()
         batched = batched_measurement(args, world, rank, dev)
+    adjoint = None
+    if not args.no_adjoint:
+        torch.cuda.empty_cache()
+        adjoint = adjoint_measurement(args, world, rank, dev)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = run_cpu_baseline(args.cpu_seconds)
@@ -466,7 +545,7 @@ def gpu_arm(args, world, rank, local_rank):
             "kernel_ms_per_step": per_kernel_ms, "kernel_fp64_frac": per_kernel_fp64,
             "kernel_hbm_frac": per_kernel_hbm,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * K, "clocks": clk, "setup_s": setup_s,
-            "device_bytes": state_bytes, "batched": batched,
+            "device_bytes": state_bytes, "batched": batched, "adjoint": adjoint,
         }
         print(json.dumps(line), flush=True)
 
