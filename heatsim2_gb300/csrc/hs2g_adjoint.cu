@@ -47,9 +47,14 @@ struct AView {
   const AInst* inst;
   const int64_t* vox_off;   // ninst + 1 voxel prefix
   const int64_t* line_off;  // 3 * (ninst + 1) line prefixes, axis-major (x, y, z)
+  const int64_t* xg_off;    // ninst + 1 prefix of x-line groups (kXL consecutive x-lines of one instance)
   int ninst;
   int64_t nvox;
 };
+
+constexpr int kXL = 32;   // x-lines per CTA of the tiled x kernels
+constexpr int kXC = 32;   // columns per chunk
+constexpr int kXT = 128;  // threads: 4 warps, 8 lines each when loading and storing a chunk
 
 inline unsigned nblk(int64_t n) { return (unsigned)std::max<int64_t>(1, (n + kTh - 1) / kTh); }
 
@@ -130,70 +135,283 @@ __global__ void adj_factor_kernel(AView v, int axis, int64_t nlines, const doubl
   }
 }
 
-// r0 = L T + s q
-__global__ void adj_residual_kernel(AView v, const double* __restrict__ T, const double* __restrict__ gx,
-                                    const double* __restrict__ gy, const double* __restrict__ gz,
-                                    const double* __restrict__ q, double s, double* __restrict__ r0) {
-  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p >= v.nvox) return;
-  const Vox x = vox_at(v, p);
-  const double Tp = T[p];
-  double r = s * q[p];
-  if (x.i > 0) r += gx[p] * (T[p - 1] - Tp);
-  if (x.i + 1 < x.nx) r += gx[p + 1] * (T[p + 1] - Tp);
-  if (x.j > 0) r += gy[p] * (T[p - x.nx] - Tp);
-  if (x.j + 1 < x.ny) r += gy[p + x.nx] * (T[p + x.nx] - Tp);
-  if (x.k > 0) r += gz[p] * (T[p - x.nxy] - Tp);
-  if (x.k + 1 < x.nz) r += gz[p + x.nxy] * (T[p + x.nxy] - Tp);
-  r0[p] = r;
+// The x-line kernels below stage 32 lines x 32 columns of each operand through shared memory: loads and
+// stores are row-contiguous (lane = column), the recurrence runs one line per lane of warp 0 (lane = line).
+// CTA b covers the x-lines [l0, l0 + nl) of one instance, a contiguous (nl, nx) block of every field.
+struct XGroup {
+  int64_t off, l0, nl, nx, ny, nz;
+};
+__device__ __forceinline__ XGroup xgroup(const AView& v, int64_t b) {
+  const int i = find_inst(v.xg_off, v.ninst, b);
+  const AInst& in = v.inst[i];
+  XGroup g;
+  g.off = in.off;
+  g.nx = in.nx;
+  g.ny = in.ny;
+  g.nz = in.nz;
+  g.l0 = (b - v.xg_off[i]) * kXL;
+  g.nl = min((int64_t)kXL, in.nz * in.ny - g.l0);
+  return g;
 }
 
-// y = A_a^-1 (scale * rhs) along each line (scale = M, or 1 when M is null); rhs may alias y (each element is
-// read before it is written).  When T_out is given, also T_out = T_in + y (T_out may alias T_in).
-__global__ void adj_solve_kernel(AView v, int axis, int64_t nlines, const double* __restrict__ M, const double* rhs,
-                                 const double* __restrict__ lo, const double* __restrict__ u,
-                                 const double* __restrict__ ip, double* y, const double* T_in, double* T_out) {
+// forward x stage fused with the residual r0 = L T + s q: y0 = A_x^-1 r0, forward elimination
+// z_r = (r0_r - lo_r z_{r-1}) / piv_r, then back substitution y_r = z_r - u_r y_{r+1}
+__global__ void __launch_bounds__(kXT) adj_xfwd_kernel(AView v, const double* __restrict__ T,
+                                                       const double* __restrict__ gx, const double* __restrict__ gy,
+                                                       const double* __restrict__ gz, const double* __restrict__ q,
+                                                       double s, const double* __restrict__ lo,
+                                                       const double* __restrict__ u, const double* __restrict__ ip,
+                                                       double* __restrict__ y0) {
+  __shared__ double sr[kXL][kXC + 1], sl[kXL][kXC + 1], si[kXL][kXC + 1];
+  const XGroup g = xgroup(v, blockIdx.x);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int kPer = kXL / (kXT / 32);
+  const int64_t nxy = g.nx * g.ny;
+  const int nch = (int)((g.nx + kXC - 1) / kXC);
+  double carry = 0.0;
+  for (int ch = 0; ch < nch; ++ch) {
+    const int64_t i = (int64_t)ch * kXC + lane;
+#pragma unroll 2
+    for (int ll = 0; ll < kPer; ++ll) {
+      const int l = warp * kPer + ll;
+      if (l < g.nl && i < g.nx) {
+        const int64_t line = g.l0 + l, j = line % g.ny, k = line / g.ny;
+        const int64_t p = g.off + line * g.nx + i;
+        const double Tp = T[p];
+        double r = s * q[p];
+        if (i > 0) r += gx[p] * (T[p - 1] - Tp);
+        if (i + 1 < g.nx) r += gx[p + 1] * (T[p + 1] - Tp);
+        if (j > 0) r += gy[p] * (T[p - g.nx] - Tp);
+        if (j + 1 < g.ny) r += gy[p + g.nx] * (T[p + g.nx] - Tp);
+        if (k > 0) r += gz[p] * (T[p - nxy] - Tp);
+        if (k + 1 < g.nz) r += gz[p + nxy] * (T[p + nxy] - Tp);
+        sr[l][lane] = r;
+        sl[l][lane] = lo[p];
+        si[l][lane] = ip[p];
+      }
+    }
+    __syncthreads();
+    if (warp == 0 && lane < g.nl) {
+      const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
+      double z = carry;
+      for (int cc = 0; cc < cw; ++cc) {
+        z = (sr[lane][cc] - sl[lane][cc] * z) * si[lane][cc];
+        sr[lane][cc] = z;
+      }
+      carry = z;
+    }
+    __syncthreads();
+    for (int ll = 0; ll < kPer; ++ll) {
+      const int l = warp * kPer + ll;
+      if (l < g.nl && i < g.nx) y0[g.off + (g.l0 + l) * g.nx + i] = sr[l][lane];
+    }
+    __syncthreads();
+  }
+  carry = 0.0;
+  for (int ch = nch - 1; ch >= 0; --ch) {
+    const int64_t i = (int64_t)ch * kXC + lane;
+    for (int ll = 0; ll < kPer; ++ll) {
+      const int l = warp * kPer + ll;
+      if (l < g.nl && i < g.nx) {
+        const int64_t p = g.off + (g.l0 + l) * g.nx + i;
+        sr[l][lane] = y0[p];
+        sl[l][lane] = u[p];
+      }
+    }
+    __syncthreads();
+    if (warp == 0 && lane < g.nl) {
+      const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
+      double x = carry;
+      for (int cc = cw - 1; cc >= 0; --cc) {
+        x = sr[lane][cc] - sl[lane][cc] * x;
+        sr[lane][cc] = x;
+      }
+      carry = x;
+    }
+    __syncthreads();
+    for (int ll = 0; ll < kPer; ++ll) {
+      const int l = warp * kPer + ll;
+      if (l < g.nl && i < g.nx) y0[g.off + (g.l0 + l) * g.nx + i] = sr[l][lane];
+    }
+    __syncthreads();
+  }
+}
+
+// transposed x stage: mu0 = A_x^-T (M mu1), the arithmetic of adj_solve_t_kernel on axis 0
+__global__ void __launch_bounds__(kXT) adj_xsolve_t_kernel(AView v, const double* __restrict__ M,
+                                                           const double* __restrict__ rhs,
+                                                           const double* __restrict__ lo,
+                                                           const double* __restrict__ u,
+                                                           const double* __restrict__ ip, double* __restrict__ mu) {
+  __shared__ double sb[kXL][kXC + 1], sl[kXL][kXC + 1], si[kXL][kXC + 1];
+  const XGroup g = xgroup(v, blockIdx.x);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int kPer = kXL / (kXT / 32);
+  const int nch = (int)((g.nx + kXC - 1) / kXC);
+  double w = 0.0, u_prev = 0.0;
+  for (int ch = 0; ch < nch; ++ch) {  // U^T w = M rhs, rows ascending
+    const int64_t i = (int64_t)ch * kXC + lane;
+    for (int ll = 0; ll < kPer; ++ll) {
+      const int l = warp * kPer + ll;
+      if (l < g.nl && i < g.nx) {
+        const int64_t p = g.off + (g.l0 + l) * g.nx + i;
+        sb[l][lane] = M[p] * rhs[p];
+        sl[l][lane] = u[p];
+      }
+    }
+    __syncthreads();
+    if (warp == 0 && lane < g.nl) {
+      const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
+      for (int cc = 0; cc < cw; ++cc) {
+        w = sb[lane][cc] - u_prev * w;
+        u_prev = sl[lane][cc];
+        sb[lane][cc] = w;
+      }
+    }
+    __syncthreads();
+    for (int ll = 0; ll < kPer; ++ll) {
+      const int l = warp * kPer + ll;
+      if (l < g.nl && i < g.nx) mu[g.off + (g.l0 + l) * g.nx + i] = sb[l][lane];
+    }
+    __syncthreads();
+  }
+  double x = 0.0, lo_next = 0.0;
+  for (int ch = nch - 1; ch >= 0; --ch) {  // Lo^T x = w, rows descending
+    const int64_t i = (int64_t)ch * kXC + lane;
+    for (int ll = 0; ll < kPer; ++ll) {
+      const int l = warp * kPer + ll;
+      if (l < g.nl && i < g.nx) {
+        const int64_t p = g.off + (g.l0 + l) * g.nx + i;
+        sb[l][lane] = mu[p];
+        sl[l][lane] = lo[p];
+        si[l][lane] = ip[p];
+      }
+    }
+    __syncthreads();
+    if (warp == 0 && lane < g.nl) {
+      const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
+      for (int cc = cw - 1; cc >= 0; --cc) {
+        x = (sb[lane][cc] - lo_next * x) * si[lane][cc];
+        lo_next = sl[lane][cc];
+        sb[lane][cc] = x;
+      }
+    }
+    __syncthreads();
+    for (int ll = 0; ll < kPer; ++ll) {
+      const int l = warp * kPer + ll;
+      if (l < g.nl && i < g.nx) mu[g.off + (g.l0 + l) * g.nx + i] = sb[l][lane];
+    }
+    __syncthreads();
+  }
+}
+
+// y / z stage, forward: y = A_a^-1 (M rhs) along each strided line (one thread per line, neighbouring
+// threads on neighbouring lines, so every row access is coalesced); T_out = T_in + y when T_out is given.
+// Rows go in blocks of kRB: the loads of a block are issued together, then the recurrence runs through it,
+// so a line pays one memory latency per block instead of one per row.
+constexpr int kRB = 8;
+
+__global__ void __launch_bounds__(128, 4) adj_ysolve_kernel(AView v, int axis, int64_t nlines, const double* __restrict__ M,
+                                  const double* __restrict__ rhs, const double* __restrict__ lo,
+                                  const double* __restrict__ u, const double* __restrict__ ip,
+                                  double* __restrict__ y, const double* __restrict__ T_in,
+                                  double* __restrict__ T_out) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= nlines) return;
   const Line ln = line_at(v, axis, t);
   double z = 0.0;
-  for (int64_t r = 0; r < ln.len; ++r) {
-    const int64_t p = ln.base + r * ln.stride;
-    const double b = M ? M[p] * rhs[p] : rhs[p];
-    z = (b - lo[p] * z) * ip[p];
-    y[p] = z;
+  for (int64_t r0 = 0; r0 < ln.len; r0 += kRB) {
+    double b[kRB], l[kRB], iv[kRB];
+#pragma unroll
+    for (int e = 0; e < kRB; ++e) {
+      if (r0 + e < ln.len) {
+        const int64_t p = ln.base + (r0 + e) * ln.stride;
+        b[e] = M[p] * rhs[p];
+        l[e] = lo[p];
+        iv[e] = ip[p];
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < kRB; ++e) {
+      if (r0 + e < ln.len) {
+        z = (b[e] - l[e] * z) * iv[e];
+        y[ln.base + (r0 + e) * ln.stride] = z;
+      }
+    }
   }
   double x = 0.0;
-  for (int64_t r = ln.len - 1; r >= 0; --r) {
-    const int64_t p = ln.base + r * ln.stride;
-    x = y[p] - u[p] * x;
-    y[p] = x;
-    if (T_out) T_out[p] = T_in[p] + x;
+  for (int64_t r1 = ln.len - 1; r1 >= 0; r1 -= kRB) {
+    double yy[kRB], uu[kRB], tt[kRB];
+#pragma unroll
+    for (int e = 0; e < kRB; ++e) {
+      if (r1 - e >= 0) {
+        const int64_t p = ln.base + (r1 - e) * ln.stride;
+        yy[e] = y[p];
+        uu[e] = u[p];
+        tt[e] = T_out ? T_in[p] : 0.0;
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < kRB; ++e) {
+      if (r1 - e >= 0) {
+        const int64_t p = ln.base + (r1 - e) * ln.stride;
+        x = yy[e] - uu[e] * x;
+        y[p] = x;
+        if (T_out) T_out[p] = tt[e] + x;
+      }
+    }
   }
 }
 
-// mu = A_a^-T (scale * rhs) along each line (scale = M, or 1 when M is null)
-__global__ void adj_solve_t_kernel(AView v, int axis, int64_t nlines, const double* __restrict__ M,
-                                   const double* __restrict__ rhs, const double* __restrict__ lo,
-                                   const double* __restrict__ u, const double* __restrict__ ip,
-                                   double* __restrict__ mu) {
+// y / z stage, transposed: mu = A_a^-T (scale * rhs) along each strided line (scale = M, or 1 when M is
+// null), rows in blocks of kRB as above
+__global__ void __launch_bounds__(128, 4) adj_ysolve_t_kernel(AView v, int axis, int64_t nlines, const double* __restrict__ M,
+                                    const double* __restrict__ rhs, const double* __restrict__ lo,
+                                    const double* __restrict__ u, const double* __restrict__ ip,
+                                    double* __restrict__ mu) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= nlines) return;
   const Line ln = line_at(v, axis, t);
   double w = 0.0, u_prev = 0.0;
-  for (int64_t r = 0; r < ln.len; ++r) {  // U^T w = b
-    const int64_t p = ln.base + r * ln.stride;
-    const double b = M ? M[p] * rhs[p] : rhs[p];
-    w = b - u_prev * w;
-    u_prev = u[p];
-    mu[p] = w;
+  for (int64_t r0 = 0; r0 < ln.len; r0 += kRB) {  // U^T w = b, rows ascending
+    double b[kRB], uu[kRB];
+#pragma unroll
+    for (int e = 0; e < kRB; ++e) {
+      if (r0 + e < ln.len) {
+        const int64_t p = ln.base + (r0 + e) * ln.stride;
+        b[e] = M ? M[p] * rhs[p] : rhs[p];
+        uu[e] = u[p];
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < kRB; ++e) {
+      if (r0 + e < ln.len) {
+        w = b[e] - u_prev * w;
+        u_prev = uu[e];
+        mu[ln.base + (r0 + e) * ln.stride] = w;
+      }
+    }
   }
   double x = 0.0, lo_next = 0.0;
-  for (int64_t r = ln.len - 1; r >= 0; --r) {  // Lo^T x = w
-    const int64_t p = ln.base + r * ln.stride;
-    x = (mu[p] - lo_next * x) * ip[p];
-    lo_next = lo[p];
-    mu[p] = x;
+  for (int64_t r1 = ln.len - 1; r1 >= 0; r1 -= kRB) {  // Lo^T x = w, rows descending
+    double ww[kRB], l[kRB], iv[kRB];
+#pragma unroll
+    for (int e = 0; e < kRB; ++e) {
+      if (r1 - e >= 0) {
+        const int64_t p = ln.base + (r1 - e) * ln.stride;
+        ww[e] = mu[p];
+        l[e] = lo[p];
+        iv[e] = ip[p];
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < kRB; ++e) {
+      if (r1 - e >= 0) {
+        x = (ww[e] - lo_next * x) * iv[e];
+        lo_next = l[e];
+        mu[ln.base + (r1 - e) * ln.stride] = x;
+      }
+    }
   }
 }
 
@@ -261,19 +479,21 @@ __device__ __forceinline__ double two_sum(double s, double v, double& err) {
   return t;
 }
 
-// misfit of step `step` per instance, as a compensated pair: part[2*(step*ninst + i)] + part[... + 1] = the sum
-// over the top layer of (T - obs)^2, accumulated with per-thread Neumaier sums and a TwoSum tree (one block of
-// 256 threads per instance, fixed order), so the loss carries no summation error that would swamp the small
-// loss differences finite-difference checks take
+// misfit of step `step`, as compensated pairs: block (c, i) sums (T - obs)^2 over its slice of instance i's
+// top layer with per-thread Neumaier sums and a TwoSum tree (256 threads, fixed order) and writes
+// part[2*((step*ninst + i)*kMisfitBlocks + c)] and the next entry (rounded sum, error); summing the pairs
+// exactly on the host leaves the loss with no summation error that would swamp the small loss differences
+// finite-difference checks take
+constexpr int kMisfitBlocks = 8;
 __global__ void adj_misfit_kernel(AView v, const double* __restrict__ T, const double* __restrict__ obs,
                                   int64_t step, double* __restrict__ part) {
   __shared__ double sh_hi[256], sh_lo[256];
-  const AInst& in = v.inst[blockIdx.x];
+  const AInst& in = v.inst[blockIdx.y];
   const int64_t m = in.ny * in.nx;
   const double* o = obs + in.obs_off + step * m;
   const double* t = T + in.off;
   double hi = 0.0, lo = 0.0;
-  for (int64_t e = threadIdx.x; e < m; e += blockDim.x) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
     const double r = t[e] - o[e];
     const double sq = r * r;
     double err;
@@ -293,7 +513,7 @@ __global__ void adj_misfit_kernel(AView v, const double* __restrict__ T, const d
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const int64_t at = 2 * (step * v.ninst + blockIdx.x);
+    const int64_t at = 2 * ((step * v.ninst + blockIdx.y) * kMisfitBlocks + blockIdx.x);
     part[at] = sh_hi[0];
     part[at + 1] = sh_lo[0];
   }
@@ -334,6 +554,8 @@ struct hs2g_adjoint {
   hs2g::AInst* inst = nullptr;
   int64_t* vox_off = nullptr;
   int64_t* line_off = nullptr;
+  int64_t* xg_off = nullptr;
+  int64_t nxgroups = 0;
   // parameters and derived fields
   double *k = nullptr, *C = nullptr, *q = nullptr, *M = nullptr;
   double* g[3] = {nullptr, nullptr, nullptr};
@@ -349,7 +571,7 @@ struct hs2g_adjoint {
   double* T = nullptr;      // forward state
   double *lam = nullptr, *mu[3] = {nullptr, nullptr, nullptr};
   double *gg[3] = {nullptr, nullptr, nullptr}, *gM = nullptr, *gq = nullptr;
-  double* parts = nullptr;  // 2 * nsteps * ninst misfit parts (compensated pairs)
+  double* parts = nullptr;  // 2 * kMisfitBlocks * nsteps * ninst misfit parts (compensated pairs)
   int64_t obs_cap = 0, ckpt_cap = 0, seg_cap = 0, parts_cap = 0;
   int64_t fixed_bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -380,7 +602,20 @@ struct AGuard {
   }
 };
 
-hs2g::AView view(const hs2g_adjoint* a) { return hs2g::AView{a->inst, a->vox_off, a->line_off, a->ninst, a->n}; }
+hs2g::AView view(const hs2g_adjoint* a) {
+  return hs2g::AView{a->inst, a->vox_off, a->line_off, a->xg_off, a->ninst, a->n};
+}
+
+// threads per CTA of the one-thread-per-line kernels: smaller CTAs when there are few lines, so that they
+// spread over every SM
+int line_threads(int64_t nlines) {
+  const int64_t want = 2 * 152;
+  return nlines >= 128 * want ? 128 : (nlines >= 64 * want ? 64 : 32);
+}
+unsigned line_blocks(int64_t nlines) {
+  const int th = line_threads(nlines);
+  return (unsigned)std::max<int64_t>(1, (nlines + th - 1) / th);
+}
 
 cudaError_t grow(double** p, int64_t* cap, int64_t need) {
   if (*p && *cap >= need) return cudaSuccess;
@@ -397,13 +632,12 @@ cudaError_t fwd_step(hs2g_adjoint* a, const double* T_in, double* T_out, double*
                      double s) {
   const hs2g::AView v = view(a);
   cudaStream_t st = a->stream;
-  hs2g::adj_residual_kernel<<<nblk(a->n), kTh, 0, st>>>(v, T_in, a->g[0], a->g[1], a->g[2], a->q, s, y0);
-  hs2g::adj_solve_kernel<<<nblk(a->nlines[0]), kTh, 0, st>>>(v, 0, a->nlines[0], nullptr, y0, a->lo[0], a->u[0],
-                                                             a->ip[0], y0, nullptr, nullptr);
-  hs2g::adj_solve_kernel<<<nblk(a->nlines[1]), kTh, 0, st>>>(v, 1, a->nlines[1], a->M, y0, a->lo[1], a->u[1],
-                                                             a->ip[1], y1, nullptr, nullptr);
-  hs2g::adj_solve_kernel<<<nblk(a->nlines[2]), kTh, 0, st>>>(v, 2, a->nlines[2], a->M, y1, a->lo[2], a->u[2],
-                                                             a->ip[2], y2, T_in, T_out);
+  hs2g::adj_xfwd_kernel<<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(v, T_in, a->g[0], a->g[1], a->g[2], a->q, s,
+                                                                      a->lo[0], a->u[0], a->ip[0], y0);
+  hs2g::adj_ysolve_kernel<<<line_blocks(a->nlines[1]), line_threads(a->nlines[1]), 0, st>>>(
+      v, 1, a->nlines[1], a->M, y0, a->lo[1], a->u[1], a->ip[1], y1, nullptr, nullptr);
+  hs2g::adj_ysolve_kernel<<<line_blocks(a->nlines[2]), line_threads(a->nlines[2]), 0, st>>>(
+      v, 2, a->nlines[2], a->M, y1, a->lo[2], a->u[2], a->ip[2], y2, T_in, T_out);
   return cudaGetLastError();
 }
 
@@ -412,12 +646,12 @@ cudaError_t bwd_step(hs2g_adjoint* a, const double* Tn, const double* y0, const 
                      double s, int64_t obs_step) {
   const hs2g::AView v = view(a);
   cudaStream_t st = a->stream;
-  hs2g::adj_solve_t_kernel<<<nblk(a->nlines[2]), kTh, 0, st>>>(v, 2, a->nlines[2], nullptr, a->lam, a->lo[2],
-                                                               a->u[2], a->ip[2], a->mu[2]);
-  hs2g::adj_solve_t_kernel<<<nblk(a->nlines[1]), kTh, 0, st>>>(v, 1, a->nlines[1], a->M, a->mu[2], a->lo[1],
-                                                               a->u[1], a->ip[1], a->mu[1]);
-  hs2g::adj_solve_t_kernel<<<nblk(a->nlines[0]), kTh, 0, st>>>(v, 0, a->nlines[0], a->M, a->mu[1], a->lo[0],
-                                                               a->u[0], a->ip[0], a->mu[0]);
+  hs2g::adj_ysolve_t_kernel<<<line_blocks(a->nlines[2]), line_threads(a->nlines[2]), 0, st>>>(
+      v, 2, a->nlines[2], nullptr, a->lam, a->lo[2], a->u[2], a->ip[2], a->mu[2]);
+  hs2g::adj_ysolve_t_kernel<<<line_blocks(a->nlines[1]), line_threads(a->nlines[1]), 0, st>>>(
+      v, 1, a->nlines[1], a->M, a->mu[2], a->lo[1], a->u[1], a->ip[1], a->mu[1]);
+  hs2g::adj_xsolve_t_kernel<<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(v, a->M, a->mu[1], a->lo[0], a->u[0],
+                                                                          a->ip[0], a->mu[0]);
   hs2g::adj_update_kernel<<<nblk(a->n), kTh, 0, st>>>(v, a->g[0], a->g[1], a->g[2], Tn, y0, y1, y2, a->mu[0],
                                                       a->mu[1], a->mu[2], s, a->obs, obs_step, a->lam, a->gg[0],
                                                       a->gg[1], a->gg[2], a->gM, a->gq);
@@ -425,7 +659,7 @@ cudaError_t bwd_step(hs2g_adjoint* a, const double* Tn, const double* y0, const 
 }
 
 void adj_free(hs2g_adjoint* a) {
-  void* ptrs[] = {a->inst, a->vox_off, a->line_off, a->k, a->C, a->q, a->M, a->g[0], a->g[1], a->g[2],
+  void* ptrs[] = {a->inst, a->vox_off, a->line_off, a->xg_off, a->k, a->C, a->q, a->M, a->g[0], a->g[1], a->g[2],
                   a->lo[0], a->lo[1], a->lo[2], a->u[0], a->u[1], a->u[2], a->ip[0], a->ip[1], a->ip[2],
                   a->obs, a->ckpts, a->seg, a->T, a->lam, a->mu[0], a->mu[1], a->mu[2], a->gg[0], a->gg[1],
                   a->gg[2], a->gM, a->gq, a->parts};
@@ -455,7 +689,7 @@ int hs2g_adjoint_create(int n, const hs2g_adjoint_grid* grids, double dt, int de
   if (n < 1 || !grids || !(dt > 0) || !std::isfinite(dt))
     return afail(HS2G_ERR_ARG, "hs2g_adjoint_create: bad argument");
   std::vector<hs2g::AInst> inst((size_t)n);
-  std::vector<int64_t> vox_off((size_t)n + 1, 0), line_off(3 * ((size_t)n + 1), 0);
+  std::vector<int64_t> vox_off((size_t)n + 1, 0), line_off(3 * ((size_t)n + 1), 0), xg_off((size_t)n + 1, 0);
   int64_t nobs = 0;
   const int64_t limit = int64_t(1) << 40;
   for (int i = 0; i < n; ++i) {
@@ -479,7 +713,9 @@ int hs2g_adjoint_create(int n, const hs2g_adjoint_grid* grids, double dt, int de
     line_off[0 * (n + 1) + i + 1] = line_off[0 * (n + 1) + i] + g.nz * g.ny;
     line_off[1 * (n + 1) + i + 1] = line_off[1 * (n + 1) + i] + g.nz * g.nx;
     line_off[2 * (n + 1) + i + 1] = line_off[2 * (n + 1) + i] + g.ny * g.nx;
+    xg_off[i + 1] = xg_off[i] + (g.nz * g.ny + hs2g::kXL - 1) / hs2g::kXL;
   }
+  if (xg_off[n] > 0x7fffffff) return afail(HS2G_ERR_ARG, "hs2g_adjoint_create: batch too large");
   AGuard guard(device);
   if (!guard.ok) return afail(HS2G_ERR_CUDA, "hs2g_adjoint_create: cannot select device");
   hs2g_adjoint* a = new hs2g_adjoint();
@@ -489,6 +725,7 @@ int hs2g_adjoint_create(int n, const hs2g_adjoint_grid* grids, double dt, int de
   a->n = vox_off[n];
   a->nobs_step = nobs;
   for (int ax = 0; ax < 3; ++ax) a->nlines[ax] = line_off[ax * (n + 1) + n];
+  a->nxgroups = xg_off[n];
   a->host_inst = inst;
   a->host_vox_off = vox_off;
   cudaError_t e = cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking);
@@ -497,6 +734,7 @@ int hs2g_adjoint_create(int n, const hs2g_adjoint_grid* grids, double dt, int de
   if (e == cudaSuccess) e = cudaMalloc(&a->inst, sizeof(hs2g::AInst) * n);
   if (e == cudaSuccess) e = cudaMalloc(&a->vox_off, sizeof(int64_t) * (n + 1));
   if (e == cudaSuccess) e = cudaMalloc(&a->line_off, sizeof(int64_t) * 3 * (n + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&a->xg_off, sizeof(int64_t) * (n + 1));
   double** per_voxel[] = {&a->k, &a->C, &a->q, &a->M, &a->g[0], &a->g[1], &a->g[2], &a->lo[0], &a->lo[1],
                           &a->lo[2], &a->u[0], &a->u[1], &a->u[2], &a->ip[0], &a->ip[1], &a->ip[2], &a->T,
                           &a->lam, &a->mu[0], &a->mu[1], &a->mu[2], &a->gg[0], &a->gg[1], &a->gg[2], &a->gM,
@@ -508,6 +746,7 @@ int hs2g_adjoint_create(int n, const hs2g_adjoint_grid* grids, double dt, int de
   if (e == cudaSuccess) e = cudaMemcpy(a->vox_off, vox_off.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(a->line_off, line_off.data(), sizeof(int64_t) * 3 * (n + 1), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(a->xg_off, xg_off.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     const int rc = acuda(e, "hs2g_adjoint_create");
     adj_free(a);
@@ -589,7 +828,7 @@ int hs2g_adjoint_forward(hs2g_adjoint* a, int nsteps, const double* schedule, co
   cudaError_t e = cudaStreamSynchronize(st);  // buffers may be reallocated below
   if (e == cudaSuccess) e = grow(&a->obs, &a->obs_cap, (int64_t)nsteps * a->nobs_step);
   if (e == cudaSuccess) e = grow(&a->ckpts, &a->ckpt_cap, nck * n);
-  if (e == cudaSuccess) e = grow(&a->parts, &a->parts_cap, (int64_t)2 * nsteps * a->ninst);
+  if (e == cudaSuccess) e = grow(&a->parts, &a->parts_cap, (int64_t)2 * hs2g::kMisfitBlocks * nsteps * a->ninst);
   if (e != cudaSuccess) return acuda(e, "hs2g_adjoint_forward: device allocation");
   std::vector<hs2g::AInst> inst = a->host_inst;
   for (auto& in : inst) in.obs_off *= nsteps;
@@ -606,23 +845,23 @@ int hs2g_adjoint_forward(hs2g_adjoint* a, int nsteps, const double* schedule, co
     // the adjoint buffers are free during the forward pass and hold the increments
     if (e == cudaSuccess) e = fwd_step(a, a->T, a->T, a->mu[0], a->mu[1], a->mu[2], a->sched[s]);
     if (e == cudaSuccess) {
-      hs2g::adj_misfit_kernel<<<a->ninst, 256, 0, st>>>(v, a->T, a->obs, s, a->parts);
+      hs2g::adj_misfit_kernel<<<dim3(hs2g::kMisfitBlocks, a->ninst), 256, 0, st>>>(v, a->T, a->obs, s, a->parts);
       e = cudaGetLastError();
     }
   }
   if (e == cudaSuccess) e = cudaEventRecord(a->ev1, st);
-  std::vector<double> parts((size_t)2 * nsteps * a->ninst);
+  std::vector<double> parts((size_t)2 * hs2g::kMisfitBlocks * nsteps * a->ninst);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(parts.data(), a->parts, sizeof(double) * parts.size(), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess && T_out) e = cudaMemcpyAsync(T_out, a->T, sizeof(double) * n, out_kind(flags), st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return acuda(e, "hs2g_adjoint_forward");
   read_elapsed(a, elapsed_ms);
-  for (int i = 0; i < a->ninst; ++i) {  // Neumaier sum of the per-step pairs
+  for (int i = 0; i < a->ninst; ++i) {  // Neumaier sum of the per-step, per-block pairs
     double acc = 0.0, comp = 0.0;
     for (int s = 0; s < nsteps; ++s)
-      for (int h = 0; h < 2; ++h) {
-        const double v = parts[2 * ((size_t)s * a->ninst + i) + h];
+      for (int h = 0; h < 2 * hs2g::kMisfitBlocks; ++h) {
+        const double v = parts[2 * ((size_t)s * a->ninst + i) * hs2g::kMisfitBlocks + h];
         const double t = acc + v;
         comp += std::fabs(acc) >= std::fabs(v) ? (acc - t) + v : (v - t) + acc;
         acc = t;
