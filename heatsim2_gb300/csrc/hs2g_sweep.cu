@@ -26,6 +26,11 @@ constexpr int kXChunk = 32;   // columns per staged chunk
 constexpr int kXThreads = 128;
 constexpr int kXWarps = kXThreads / 32;
 constexpr int kXLinesPerWarp = kXLines / kXWarps;
+// Register budget of the x sweep: at 72 registers 7 CTAs of 128 threads fit on an SM, so the 1040 CTAs of a
+// 65 x 512-line grid run in one wave on 152 SMs with the most loads in flight per thread (334 us at
+// 65x512x512; 80 registers: 6 CTAs per SM and a second wave, 530 us; the compiler's own choice of 48
+// registers: 415 us).
+constexpr int kXMinBlocks = 6;
 constexpr int kLineThreads = 128;
 
 // Stage-0 right-hand side of voxel (L, i) of x-line L = k*ny + j, pre-scaled by the line's pivot:
@@ -64,7 +69,7 @@ __device__ __forceinline__ double stencil_x(const Dims& d, const double* __restr
 }
 
 template <bool HAS_Q>
-__global__ void __launch_bounds__(kXThreads) sweep_x_kernel(Dims d, const double* __restrict__ T, Coeffs c,
+__global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d, const double* __restrict__ T, Coeffs c,
                                                              const uint8_t* __restrict__ vclass,
                                                              const double* __restrict__ qdense, QTable qt,
                                                              double* __restrict__ W0) {
@@ -97,12 +102,13 @@ __global__ void __launch_bounds__(kXThreads) sweep_x_kernel(Dims d, const double
       sa[l][lane] = a;
     }
     __syncthreads();
-    if (warp == 0) {
+    if (warp * 32 + lane < kXLines) {  // lane = line of the recurrence
+      const int l = warp * 32 + lane;
       const int cw = (int)min((int64_t)kXChunk, d.nx - (int64_t)ch * kXChunk);
       double z = carry;
       for (int cc = 0; cc < cw; ++cc) {
-        z = fma(-sa[lane][cc], z, sr[lane][cc]);
-        sr[lane][cc] = z;
+        z = fma(-sa[l][cc], z, sr[l][cc]);
+        sr[l][cc] = z;
       }
       carry = z;
     }
@@ -134,12 +140,13 @@ __global__ void __launch_bounds__(kXThreads) sweep_x_kernel(Dims d, const double
       sa[l][lane] = b;
     }
     __syncthreads();
-    if (warp == 0) {
+    if (warp * 32 + lane < kXLines) {
+      const int l = warp * 32 + lane;
       const int cw = (int)min((int64_t)kXChunk, d.nx - (int64_t)ch * kXChunk);
       double x = carry;
       for (int cc = cw - 1; cc >= 0; --cc) {
-        x = fma(-sa[lane][cc], x, sr[lane][cc]);
-        sr[lane][cc] = x;
+        x = fma(-sa[l][cc], x, sr[l][cc]);
+        sr[l][cc] = x;
       }
       carry = x;
     }
