@@ -59,6 +59,8 @@ def parse_args():
     ap.add_argument("--batch-instances", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=100)
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=None,
+                    help="steps of both adjoint workloads (default: their own 500 and 400; smaller for profiling)")
     ap.add_argument("--adjoint-loop", type=int, default=32,
                     help="instances of the batched adjoint workload timed as a loop of single-instance adjoints")
     ap.add_argument("--cpu-worker", default=None, help=argparse.SUPPRESS)
@@ -362,7 +364,8 @@ def adjoint_measurement(args, world, rank, dev):
     from heatsim2_gb300.batch import shard
 
     out = {}
-    w = W.adjoint_steel()
+    steps_kw = {} if args.adjoint_steps is None else {"nsteps": args.adjoint_steps}
+    w = W.adjoint_steel(**steps_kw)
     a = Adjoint([(w["shape"], w["spacing"])], w["dt"])
     a.set_parameters(w["k"], w["C"], w["q"])
     for _ in range(2):  # warm-up, then the timed evaluation
@@ -370,12 +373,13 @@ def adjoint_measurement(args, world, rank, dev):
         a.backward()
     fwd, bwd = a.forward_ms, a.backward_ms
     vox = int(np.prod(w["shape"]))
-    out["steel"] = {"workload": "steel (32,128,128) lognormal k, 500 steps dt=10 ms, checkpoint 50",
+    out["steel"] = {"workload": "steel (32,128,128) lognormal k, %d steps dt=10 ms, checkpoint %d"
+                                % (w["nsteps"], w["ckpt"]),
                     "gradient_evals_per_s": 1e3 / (fwd + bwd), "forward_ms": fwd, "backward_ms": bwd,
                     "forward_voxel_steps_per_s": vox * w["nsteps"] / (fwd * 1e-3),
                     "device_bytes": a.device_bytes}
     del a
-    insts_all = W.adjoint_batch()
+    insts_all = W.adjoint_batch(**steps_kw)
     sizes = [int(np.prod(x["shape"])) for x in insts_all]
     insts = [insts_all[i] for i in shard(sizes, world, rank)]
     b = Adjoint([(x["shape"], x["spacing"]) for x in insts], insts[0]["dt"])
@@ -407,8 +411,8 @@ def adjoint_measurement(args, world, rank, dev):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         batch_evals = len(insts_all) / (float(t[0]) * 1e-3)
         loop_evals = len(insts_all) / (float(t[1]) * 1e-3)
-    out["batched"] = {"workload": "%d uneven two-phase instances (nz 24..48, ny,nx 96..192), 400 steps dt=5 ms, "
-                                  "checkpoint 40" % len(insts_all),
+    out["batched"] = {"workload": "%d uneven two-phase instances (nz 24..48, ny,nx 96..192), %d steps dt=5 ms, "
+                                  "checkpoint %d" % (len(insts_all), insts[0]["nsteps"], insts[0]["ckpt"]),
                       "voxels": sum(sizes), "gradient_evals_per_s": batch_evals, "ms_per_eval_batch": batch_ms,
                       "device_bytes": bytes_b,
                       "single_loop": {"gradient_evals_per_s": loop_evals, "instances_timed": nloop,
