@@ -568,11 +568,14 @@ struct hs2g_adjoint {
   double* obs = nullptr;    // nsteps * nobs_step
   double* ckpts = nullptr;  // ceil(nsteps / ckpt) * n
   double* seg = nullptr;    // ckpt * 4 * n: T, y0, y1, y2 of each step of a segment
+  double* seg2 = nullptr;   // a second segment store: the next segment is recomputed while this one is swept
+  cudaStream_t rec_stream = nullptr;  // the recompute stream
+  cudaEvent_t ev_rec[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr}, ev_start = nullptr;
   double* T = nullptr;      // forward state
   double *lam = nullptr, *mu[3] = {nullptr, nullptr, nullptr};
   double *gg[3] = {nullptr, nullptr, nullptr}, *gM = nullptr, *gq = nullptr;
   double* parts = nullptr;  // 2 * kMisfitBlocks * nsteps * ninst misfit parts (compensated pairs)
-  int64_t obs_cap = 0, ckpt_cap = 0, seg_cap = 0, parts_cap = 0;
+  int64_t obs_cap = 0, ckpt_cap = 0, seg_cap = 0, seg2_cap = 0, parts_cap = 0;
   int64_t fixed_bytes = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
@@ -627,11 +630,10 @@ cudaError_t grow(double** p, int64_t* cap, int64_t need) {
   return e;
 }
 
-// one forward step T_in -> T_out keeping y0, y1, y2 (T_out may alias T_in)
-cudaError_t fwd_step(hs2g_adjoint* a, const double* T_in, double* T_out, double* y0, double* y1, double* y2,
-                     double s) {
+// one forward step T_in -> T_out on stream st keeping y0, y1, y2 (T_out may alias T_in; NULL skips it)
+cudaError_t fwd_step(hs2g_adjoint* a, cudaStream_t st, const double* T_in, double* T_out, double* y0, double* y1,
+                     double* y2, double s) {
   const hs2g::AView v = view(a);
-  cudaStream_t st = a->stream;
   hs2g::adj_xfwd_kernel<<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(v, T_in, a->g[0], a->g[1], a->g[2], a->q, s,
                                                                       a->lo[0], a->u[0], a->ip[0], y0);
   hs2g::adj_ysolve_kernel<<<line_blocks(a->nlines[1]), line_threads(a->nlines[1]), 0, st>>>(
@@ -661,12 +663,16 @@ cudaError_t bwd_step(hs2g_adjoint* a, const double* Tn, const double* y0, const 
 void adj_free(hs2g_adjoint* a) {
   void* ptrs[] = {a->inst, a->vox_off, a->line_off, a->xg_off, a->k, a->C, a->q, a->M, a->g[0], a->g[1], a->g[2],
                   a->lo[0], a->lo[1], a->lo[2], a->u[0], a->u[1], a->u[2], a->ip[0], a->ip[1], a->ip[2],
-                  a->obs, a->ckpts, a->seg, a->T, a->lam, a->mu[0], a->mu[1], a->mu[2], a->gg[0], a->gg[1],
+                  a->obs, a->ckpts, a->seg, a->seg2, a->T, a->lam, a->mu[0], a->mu[1], a->mu[2], a->gg[0], a->gg[1],
                   a->gg[2], a->gM, a->gq, a->parts};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (a->ev0) cudaEventDestroy(a->ev0);
   if (a->ev1) cudaEventDestroy(a->ev1);
+  cudaEvent_t evs[] = {a->ev_rec[0], a->ev_rec[1], a->ev_done[0], a->ev_done[1], a->ev_start};
+  for (cudaEvent_t ev : evs)
+    if (ev) cudaEventDestroy(ev);
+  if (a->rec_stream) cudaStreamDestroy(a->rec_stream);
   if (a->stream && a->own_stream) cudaStreamDestroy(a->stream);
 }
 
@@ -731,6 +737,12 @@ int hs2g_adjoint_create(int n, const hs2g_adjoint_grid* grids, double dt, int de
   cudaError_t e = cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&a->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&a->ev1);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&a->rec_stream, cudaStreamNonBlocking);
+  for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+    e = cudaEventCreateWithFlags(&a->ev_rec[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&a->ev_done[b], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&a->ev_start, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&a->inst, sizeof(hs2g::AInst) * n);
   if (e == cudaSuccess) e = cudaMalloc(&a->vox_off, sizeof(int64_t) * (n + 1));
   if (e == cudaSuccess) e = cudaMalloc(&a->line_off, sizeof(int64_t) * 3 * (n + 1));
@@ -785,7 +797,8 @@ int hs2g_adjoint_layout(const hs2g_adjoint* a, int64_t* offsets) {
 
 int64_t hs2g_adjoint_device_bytes(const hs2g_adjoint* a) {
   if (!a) return 0;
-  return a->fixed_bytes + (int64_t)sizeof(double) * (a->obs_cap + a->ckpt_cap + a->seg_cap + a->parts_cap);
+  return a->fixed_bytes +
+         (int64_t)sizeof(double) * (a->obs_cap + a->ckpt_cap + a->seg_cap + a->seg2_cap + a->parts_cap);
 }
 
 int hs2g_adjoint_set_parameters(hs2g_adjoint* a, const double* k, const double* C, const double* q, int flags) {
@@ -843,7 +856,7 @@ int hs2g_adjoint_forward(hs2g_adjoint* a, int nsteps, const double* schedule, co
       e = cudaMemcpyAsync(a->ckpts + (int64_t)(s / ckpt) * n, a->T, sizeof(double) * n, cudaMemcpyDeviceToDevice,
                           st);
     // the adjoint buffers are free during the forward pass and hold the increments
-    if (e == cudaSuccess) e = fwd_step(a, a->T, a->T, a->mu[0], a->mu[1], a->mu[2], a->sched[s]);
+    if (e == cudaSuccess) e = fwd_step(a, st, a->T, a->T, a->mu[0], a->mu[1], a->mu[2], a->sched[s]);
     if (e == cudaSuccess) {
       hs2g::adj_misfit_kernel<<<dim3(hs2g::kMisfitBlocks, a->ninst), 256, 0, st>>>(v, a->T, a->obs, s, a->parts);
       e = cudaGetLastError();
@@ -882,9 +895,17 @@ int hs2g_adjoint_backward(hs2g_adjoint* a, double* gk, double* gC, double* gq, d
   const hs2g::AView v = view(a);
   const int64_t n = a->n;
   const int N = a->nsteps, C = a->ckpt;
-  // the segment store (T, y0, y1, y2 of ckpt steps) exists only while gradients are taken
+  // the segment stores (T, y0, y1, y2 of ckpt steps) exist only while gradients are taken; with two of them
+  // the recompute of segment sg-1 (rec_stream) runs while segment sg is swept backwards (the handle's stream)
   cudaError_t e = grow(&a->seg, &a->seg_cap, (int64_t)C * 4 * n);
   if (e != cudaSuccess) return acuda(e, "hs2g_adjoint_backward: device allocation");
+  const int nseg = (N + C - 1) / C;
+  bool dbl = false;
+  if (nseg > 1) {
+    dbl = grow(&a->seg2, &a->seg2_cap, (int64_t)C * 4 * n) == cudaSuccess;
+    if (!dbl) cudaGetLastError();  // out of memory for the second store: recompute and sweep in turn
+  }
+  double* bufs[2] = {a->seg, dbl ? a->seg2 : a->seg};
   e = cudaEventRecord(a->ev0, st);
   double* zero_list[] = {a->gg[0], a->gg[1], a->gg[2], a->gM, a->gq};
   for (double* p : zero_list)
@@ -893,21 +914,39 @@ int hs2g_adjoint_backward(hs2g_adjoint* a, double* gk, double* gC, double* gq, d
     hs2g::adj_seed_kernel<<<nblk(n), kTh, 0, st>>>(v, a->T, a->obs, N - 1, a->lam);
     e = cudaGetLastError();
   }
-  const int nseg = (N + C - 1) / C;
-  for (int sg = nseg - 1; sg >= 0 && e == cudaSuccess; --sg) {
+  cudaStream_t rs = dbl ? a->rec_stream : st;
+  if (e == cudaSuccess && dbl) e = cudaEventRecord(a->ev_start, st);  // checkpoints and parameters are ready
+  if (e == cudaSuccess && dbl) e = cudaStreamWaitEvent(rs, a->ev_start, 0);
+  // recompute segment sg into its store: slot j holds T, y0, y1, y2 of step s0 + j (the end state is not kept)
+  auto recompute = [&](int sg) -> cudaError_t {
     const int s0 = sg * C, s1 = std::min(N, s0 + C);
-    // recompute the segment: slot j holds T, y0, y1, y2 of step s0 + j; the end state is not needed
-    e = cudaMemcpyAsync(a->seg, a->ckpts + (int64_t)sg * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, st);
-    for (int s = s0; s < s1 && e == cudaSuccess; ++s) {
-      double* slot = a->seg + (int64_t)(s - s0) * 4 * n;
-      double* next = s + 1 < s1 ? slot + 4 * n : a->mu[0];
-      e = fwd_step(a, slot, next, slot + n, slot + 2 * n, slot + 3 * n, a->sched[s]);
+    double* buf = bufs[sg & 1];
+    cudaError_t r = cudaMemcpyAsync(buf, a->ckpts + (int64_t)sg * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, rs);
+    for (int s = s0; s < s1 && r == cudaSuccess; ++s) {
+      double* slot = buf + (int64_t)(s - s0) * 4 * n;
+      double* next = s + 1 < s1 ? slot + 4 * n : nullptr;
+      r = fwd_step(a, rs, slot, next, slot + n, slot + 2 * n, slot + 3 * n, a->sched[s]);
     }
+    if (r == cudaSuccess && dbl) r = cudaEventRecord(a->ev_rec[sg & 1], rs);
+    return r;
+  };
+  if (e == cudaSuccess) e = recompute(nseg - 1);
+  for (int sg = nseg - 1; sg >= 0 && e == cudaSuccess; --sg) {
+    if (dbl && sg >= 1) {
+      // store (sg-1)&1 was last read by the sweep of segment sg+1
+      e = cudaStreamWaitEvent(rs, a->ev_done[(sg - 1) & 1], 0);
+      if (e == cudaSuccess) e = recompute(sg - 1);
+    }
+    if (e == cudaSuccess && dbl) e = cudaStreamWaitEvent(st, a->ev_rec[sg & 1], 0);
+    const int s0 = sg * C, s1 = std::min(N, s0 + C);
+    const double* buf = bufs[sg & 1];
     for (int s = s1 - 1; s >= s0 && e == cudaSuccess; --s) {
-      const double* slot = a->seg + (int64_t)(s - s0) * 4 * n;
+      const double* slot = buf + (int64_t)(s - s0) * 4 * n;
       // T_s (s >= 1) is the state observed after step s - 1
       e = bwd_step(a, slot, slot + n, slot + 2 * n, slot + 3 * n, a->sched[s], s >= 1 ? s - 1 : -1);
     }
+    if (e == cudaSuccess && dbl) e = cudaEventRecord(a->ev_done[sg & 1], st);
+    if (e == cudaSuccess && !dbl && sg >= 1) e = recompute(sg - 1);
   }
   if (e == cudaSuccess) {
     hs2g::adj_chain_kernel<<<nblk(n), kTh, 0, st>>>(v, a->gg[0], a->gg[1], a->gg[2], a->gM, 1.0 / a->dt, a->mu[0],

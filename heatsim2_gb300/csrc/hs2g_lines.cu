@@ -30,8 +30,10 @@ namespace hs2g {
 namespace {
 
 constexpr int kNL = 64;        // lines per CTA (threads)
-constexpr int kRows = 8;       // rows per tile
-constexpr int kSlots = 6;      // tiles in flight per array
+constexpr int kRows = 16;      // rows per tile
+constexpr int kSlots = 2;      // tiles in flight per array (32 KB of shared memory per y CTA, so all 520
+                               // CTAs of a 65 x 512 x 512 y sweep are resident at once: 119.5 us, against
+                               // 129.5 us with 6 slots of 8 rows and 122 us with 4 slots of 8 rows)
 constexpr uint64_t kWaitNs = 2000000000ull;
 constexpr uint32_t kTileBytes = kNL * kRows * 8;
 
