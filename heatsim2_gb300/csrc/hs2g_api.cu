@@ -13,6 +13,15 @@
 using hs2g::Coeffs;
 using hs2g::Dims;
 
+// A host-buffer step (hs2g_step without HS2G_DEVICE) uploads T in kCopyChunks slabs of planes of shrinking
+// size, starting the x sweep of each slab's planes (on a stream of its own: an x CTA is latency-bound for the
+// whole length of its lines, so slabs must not wait for one another) as soon as the slab and the plane after
+// it have arrived, and downloads T' in kCopyChunks blocks of rows, each as soon as the z sweep has finished
+// its columns.  The host link (~0.2 TB/s each way on GB300) is then busy while the sweeps run.
+constexpr int kCopyChunks = 4;
+constexpr double kSlabEnd[kCopyChunks] = {0.55, 0.80, 0.93, 1.0};  // upload slab c ends at this fraction of nz
+constexpr int64_t kPipelineMinVoxels = int64_t(1) << 20;
+
 struct hs2g_handle {
   int device = 0;
   Dims d{0, 0, 0};
@@ -42,6 +51,11 @@ struct hs2g_handle {
   bool bulk_y = false, bulk_z = false;
   hs2g::TensorMapCache* tmaps = nullptr;
   int64_t bytes = 0;
+  // host-buffer steps overlap their copies with the sweeps: a copy stream, one stream per upload slab for
+  // its x sweep, and per-chunk events
+  cudaStream_t copy_stream = nullptr;
+  cudaStream_t x_stream[kCopyChunks] = {};
+  cudaEvent_t ev_in[kCopyChunks] = {}, ev_x[kCopyChunks] = {}, ev_out[kCopyChunks] = {}, ev_begin = nullptr;
 };
 
 namespace {
@@ -249,6 +263,71 @@ int ensure_staging(hs2g_handle* h) {
   return HS2G_OK;
 }
 
+int ensure_copy_pipeline(hs2g_handle* h) {
+  if (h->copy_stream) return HS2G_OK;
+  cudaError_t e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking);
+  for (int c = 0; c < kCopyChunks && e == cudaSuccess; ++c) {
+    e = cudaStreamCreateWithFlags(&h->x_stream[c], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_in[c], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_x[c], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_out[c], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_begin, cudaEventDisableTiming);
+  if (e != cudaSuccess) return cuda_fail(e, "copy pipeline");
+  return HS2G_OK;
+}
+
+// One step from host T_in to host T_out with the copies overlapped (see kCopyChunks).  Slab c of the upload
+// holds planes [k_c, k_{c+1}); once it is in, the x sweep can run on x-lines of planes up to k_{c+1} - 2 (an
+// x-line reads the planes above and below it).  The z sweep runs in blocks of rows j, each block's columns
+// complete after its launch, and a 2-D copy takes those rows of every plane back to the host.
+int step_host_pipelined(hs2g_handle* h, hs2g::StepArgs& a, const hs2g::QTable& q, const double* T_in,
+                        double* T_out) {
+  const Dims& d = h->d;
+  cudaStream_t s = h->stream, cs = h->copy_stream;
+  const int nout = (int)std::min<int64_t>(kCopyChunks, d.ny / 4);
+  const size_t plane = sizeof(double) * (size_t)d.nxy();
+  // the copy and x streams start after everything queued on the step stream so far (e.g. source uploads)
+  HS2G_CUDA(cudaEventRecord(h->ev_begin, s), "pipeline begin");
+  HS2G_CUDA(cudaStreamWaitEvent(cs, h->ev_begin, 0), "pipeline begin");
+  int64_t k0 = 0, done = 0;  // planes [0, k0) are queued for upload; x-lines [0, done) for the x sweep
+  for (int c = 0; c < kCopyChunks; ++c) {
+    const int64_t k1 = c + 1 == kCopyChunks ? d.nz : std::min<int64_t>(d.nz, std::max<int64_t>(
+                                                          k0 + 2, (int64_t)(kSlabEnd[c] * (double)d.nz)));
+    if (k1 > k0) {
+      HS2G_CUDA(cudaMemcpyAsync(h->Tin_dev + k0 * d.nxy(), T_in + k0 * d.nxy(), plane * (size_t)(k1 - k0),
+                                cudaMemcpyHostToDevice, cs), "upload T");
+    }
+    HS2G_CUDA(cudaEventRecord(h->ev_in[c], cs), "upload T");
+    cudaStream_t xs = h->x_stream[c];
+    HS2G_CUDA(cudaStreamWaitEvent(xs, h->ev_begin, 0), "upload T");
+    HS2G_CUDA(cudaStreamWaitEvent(xs, h->ev_in[c], 0), "upload T");
+    const int64_t upto = (k1 == d.nz ? d.nz : k1 - 1) * d.ny;
+    cudaError_t e = hs2g::launch_x_range(a, h->c, q, done, upto, xs);
+    if (e != cudaSuccess) return cuda_fail(e, "x sweep");
+    HS2G_CUDA(cudaEventRecord(h->ev_x[c], xs), "x sweep");
+    HS2G_CUDA(cudaStreamWaitEvent(s, h->ev_x[c], 0), "x sweep");
+    done = upto;
+    k0 = k1;
+  }
+  cudaError_t e = hs2g::launch_y(a, h->c, s);
+  if (e != cudaSuccess) return cuda_fail(e, "y sweep");
+  for (int c = 0; c < nout; ++c) {
+    const int64_t j0 = d.ny * c / nout, j1 = d.ny * (c + 1) / nout;
+    e = hs2g::launch_z_range(a, h->c, j0 * d.nx, j1 * d.nx, s);
+    if (e != cudaSuccess) return cuda_fail(e, "z sweep");
+    HS2G_CUDA(cudaEventRecord(h->ev_out[c], s), "download T");
+    HS2G_CUDA(cudaStreamWaitEvent(cs, h->ev_out[c], 0), "download T");
+    HS2G_CUDA(cudaMemcpy2DAsync(T_out + j0 * d.nx, plane, h->Tout_dev + j0 * d.nx, plane,
+                                sizeof(double) * (size_t)((j1 - j0) * d.nx), (size_t)d.nz, cudaMemcpyDeviceToHost,
+                                cs),
+              "download T");
+  }
+  HS2G_CUDA(cudaStreamSynchronize(cs), "step");
+  HS2G_CUDA(cudaStreamSynchronize(s), "step");
+  return check_status(h);
+}
+
 }  // namespace
 
 int hs2g::set_last_error(int code, const char* message) { return fail(code, "%s", message); }
@@ -283,6 +362,17 @@ void hs2g_destroy(hs2g_handle* h) {
   dfree(h, h->qdense_dev, n);
   dfree(h, h->hist_dev, 0);
   dfree(h, h->err_dev, 1);
+  if (h->copy_stream) {
+    cudaStreamSynchronize(h->copy_stream);
+    cudaStreamDestroy(h->copy_stream);
+  }
+  for (int c = 0; c < kCopyChunks; ++c) {
+    if (h->x_stream[c]) cudaStreamDestroy(h->x_stream[c]);
+    if (h->ev_in[c]) cudaEventDestroy(h->ev_in[c]);
+    if (h->ev_x[c]) cudaEventDestroy(h->ev_x[c]);
+    if (h->ev_out[c]) cudaEventDestroy(h->ev_out[c]);
+  }
+  if (h->ev_begin) cudaEventDestroy(h->ev_begin);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
 }
@@ -498,10 +588,15 @@ int hs2g_step(hs2g_handle* h, const double* T_in, double* T_out, const double* q
       a.qdense = h->qdense_dev;
     }
   }
-  if (!dev)
-    HS2G_CUDA(cudaMemcpyAsync(h->Tin_dev, T_in, sizeof(double) * n, cudaMemcpyHostToDevice, s), "upload T");
   a.T_in = Tin_d;
   a.T_out = Tout_d;
+  if (!dev && !a.bulk_z && n >= kPipelineMinVoxels && d.nz >= 8 && d.ny >= 8) {
+    int rc = ensure_copy_pipeline(h);
+    if (rc) return rc;
+    return step_host_pipelined(h, a, q, T_in, T_out);
+  }
+  if (!dev)
+    HS2G_CUDA(cudaMemcpyAsync(h->Tin_dev, T_in, sizeof(double) * n, cudaMemcpyHostToDevice, s), "upload T");
   cudaError_t e = hs2g::launch_step(a, h->c, q, s);
   if (e != cudaSuccess) return cuda_fail(e, "step kernels");
   if (!dev) {

@@ -93,5 +93,11 @@ cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable&
                                cudaEvent_t ev[4]);
 cudaError_t fp64_fma_rate(double* fma_per_s);
 cudaError_t launch_copy_layer(const Dims& d, const double* T, int layer, double* dst, cudaStream_t s);
+// the step in pieces, for overlapping host copies with it: the x sweep over x-lines [line_begin, line_end)
+// (line = k*ny + j), the whole y sweep, the plain z sweep over columns [col_begin, col_end) (col = j*nx + i)
+cudaError_t launch_x_range(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_begin,
+                           int64_t line_end, cudaStream_t s);
+cudaError_t launch_y(const StepArgs& a, const Coeffs& c, cudaStream_t s);
+cudaError_t launch_z_range(const StepArgs& a, const Coeffs& c, int64_t col_begin, int64_t col_end, cudaStream_t s);
 
 }  // namespace hs2g

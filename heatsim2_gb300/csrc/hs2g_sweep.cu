@@ -29,7 +29,9 @@ constexpr int kXLinesPerWarp = kXLines / kXWarps;
 // Register budget of the x sweep: at 72 registers 7 CTAs of 128 threads fit on an SM, so the 1040 CTAs of a
 // 65 x 512-line grid run in one wave on 152 SMs with the most loads in flight per thread (334 us at
 // 65x512x512; 80 registers: 6 CTAs per SM and a second wave, 530 us; the compiler's own choice of 48
-// registers: 415 us).
+// registers: 415 us).  A bound of 6 blocks gives the whole-grid instance 72 registers and its fastest code
+// (a bound of 7 also gives 72 registers but scheduled differently: 347-363 us); check -Xptxas -v after a
+// change.
 constexpr int kXMinBlocks = 6;
 constexpr int kLineThreads = 128;
 
@@ -68,11 +70,15 @@ __device__ __forceinline__ double stencil_x(const Dims& d, const double* __restr
   return r;
 }
 
-template <bool HAS_Q>
+// RANGED: the launch covers x-lines [line_begin, line_end) (the overlapped host-buffer step); otherwise all
+// nz*ny lines, with the arguments unused -- the two are separate instances so that the whole-grid kernel keeps
+// its own register allocation.
+template <bool HAS_Q, bool RANGED>
 __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d, const double* __restrict__ T, Coeffs c,
                                                              const uint8_t* __restrict__ vclass,
                                                              const double* __restrict__ qdense, QTable qt,
-                                                             double* __restrict__ W0) {
+                                                             double* __restrict__ W0, int64_t line_begin,
+                                                             int64_t line_end) {
   __shared__ double sr[kXLines][kXChunk + 1];
   __shared__ double sa[kXLines][kXChunk + 1];
   __shared__ double sq[HAS_Q ? HS2G_MAX_CLASSES : 1];
@@ -80,8 +86,8 @@ __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d,
   if (HAS_Q) {
     for (int e = threadIdx.x; e < HS2G_MAX_CLASSES; e += kXThreads) sq[e] = qt.q[e];
   }
-  const int64_t nlines = d.nz * d.ny;
-  const int64_t L0 = (int64_t)blockIdx.x * kXLines;
+  const int64_t nlines = RANGED ? line_end : d.nz * d.ny;
+  const int64_t L0 = (RANGED ? line_begin : 0) + (int64_t)blockIdx.x * kXLines;
   const int nchunks = (int)((d.nx + kXChunk - 1) / kXChunk);
   __syncthreads();
 
@@ -190,10 +196,12 @@ __global__ void __launch_bounds__(kLineThreads) sweep_y_kernel(Dims d, const dou
 __global__ void __launch_bounds__(kLineThreads) sweep_z_kernel(Dims d, const double* __restrict__ W1,
                                                                 const double* __restrict__ a2,
                                                                 const double* __restrict__ b2, const double* T_in,
-                                                                double* __restrict__ Z, double* T_out) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+                                                                double* __restrict__ Z, double* T_out,
+                                                                int64_t col_begin, int64_t col_end) {
+  // this launch covers the z-lines (columns j*nx + i) [col_begin, col_end)
+  const int64_t t = col_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nxy = d.nxy();
-  if (t >= nxy) return;
+  if (t >= col_end) return;
   int64_t p = t;
   double z = 0.0;
 #pragma unroll 4
@@ -271,9 +279,9 @@ cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable&
   const unsigned gx = blocks(d.nz * d.ny, kXLines);
   if (ev) cudaEventRecord(ev[0], s);
   if (has_q)
-    sweep_x_kernel<true><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0);
+    sweep_x_kernel<true, false><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0, 0, 0);
   else
-    sweep_x_kernel<false><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0);
+    sweep_x_kernel<false, false><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0, 0, 0);
   if (ev) cudaEventRecord(ev[1], s);
   cudaError_t e = cudaSuccess;
   if (a.bulk_y)
@@ -286,7 +294,7 @@ cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable&
     e = launch_lines_bulk(d, 2, a.W1, c.a2, a.W0, c.b2, a.T_in, a.T_out, a.status, a.tmaps, s);
   else
     sweep_z_kernel<<<blocks(d.nxy(), kLineThreads), kLineThreads, 0, s>>>(d, a.W1, c.a2, c.b2, a.T_in, a.W0,
-                                                                           a.T_out);
+                                                                           a.T_out, 0, d.nxy());
   if (e != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[3], s);
   return cudaGetLastError();
@@ -294,6 +302,35 @@ cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable&
 
 cudaError_t launch_step(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s) {
   return launch_step_events(a, c, q, s, nullptr);
+}
+
+cudaError_t launch_x_range(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_begin,
+                           int64_t line_end, cudaStream_t s) {
+  const Dims& d = a.d;
+  if (line_end <= line_begin) return cudaSuccess;
+  const unsigned gx = blocks(line_end - line_begin, kXLines);
+  if (a.has_qtab || a.qdense != nullptr)
+    sweep_x_kernel<true, true><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0, line_begin,
+                                                        line_end);
+  else
+    sweep_x_kernel<false, true><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0, line_begin,
+                                                         line_end);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_y(const StepArgs& a, const Coeffs& c, cudaStream_t s) {
+  const Dims& d = a.d;
+  if (a.bulk_y) return launch_lines_bulk(d, 1, a.W0, c.a1, a.W1, c.b1, nullptr, a.W1, a.status, a.tmaps, s);
+  sweep_y_kernel<<<blocks(d.nz * d.nx, kLineThreads), kLineThreads, 0, s>>>(d, a.W0, c.a1, c.b1, a.W1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_z_range(const StepArgs& a, const Coeffs& c, int64_t col_begin, int64_t col_end, cudaStream_t s) {
+  const Dims& d = a.d;
+  if (col_end <= col_begin) return cudaSuccess;
+  sweep_z_kernel<<<blocks(col_end - col_begin, kLineThreads), kLineThreads, 0, s>>>(d, a.W1, c.a2, c.b2, a.T_in,
+                                                                                   a.W0, a.T_out, col_begin, col_end);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_copy_layer(const Dims& d, const double* T, int layer, double* dst, cudaStream_t s) {

@@ -50,6 +50,25 @@ def test_device_tensor_path_equals_host_path(cuda_ok):
     assert rel_err(T.cpu().numpy(), ref[50]) <= TOL
 
 
+@pytest.mark.parametrize("shape", [(16, 256, 256), (17, 250, 240)])
+def test_overlapped_host_copies_equal_device_path(cuda_ok, shape):
+    """Host-buffer steps of >= 2^20 voxels upload in slabs of planes and download in blocks of rows while the
+    sweeps run; the result is the device path's bit for bit (uneven slab and block sizes included)."""
+    import torch
+    nz, ny, nx = shape
+    spec = W.composite_panel(seed=4, nz=nz, ny=ny, nx=nx, top_layers=4, width_range=(10, 40), depth_range=(2, 10),
+                             nsteps=3)
+    assert W.voxels(spec) >= 1 << 20
+    P, S = _setup(spec)
+    vol = W.volumetric_tuple(hs, spec)
+    times = W.step_times(spec)
+    host = _run_host(spec, times, P, S)
+    T = torch.from_numpy(W.initial_temperature(spec)).cuda()
+    for t in times:
+        T = hs.run_adi_steps(P, S, t, spec["dt"], T, spec["arrays"]["volumetric"], vol)
+    np.testing.assert_array_equal(T.cpu().numpy(), host[len(times)])
+
+
 def test_run_equals_single_steps_and_records_history(cuda_ok):
     spec, times, ref = load_golden(GOLDEN + "/sources_small.npz")
     P, S = _setup(spec)
