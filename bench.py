@@ -41,6 +41,17 @@ SEED = 1
 BYTES_PER_VOXEL = {"sweep_x": 8 + 9 * 8 + 8, "sweep_y": 4 * 8, "sweep_z": 5 * 8}
 FP64_OPS_PER_VOXEL = {"sweep_x": 9, "sweep_y": 2, "sweep_z": 3}
 KERNELS = ("sweep_x", "sweep_y", "sweep_z")
+# adjoint: arrays touched per voxel and step (8 B each), from the kernels of hs2g_adjoint.cu
+#   forward step (forward pass, and again as the recompute of the backward pass): x stage reads T, gx, gy, gz,
+#   q, lo0, ip0, u0 and writes y0 (9); y stage reads M, y0, lo1, ip1, u1, writes y1 (6); z stage reads M, y1,
+#   lo2, ip2, u2, T, writes y2, T' (8)                                                       -> 23 arrays
+#   reverse step: transposed z reads lambda, u2, lo2, ip2, writes mu2 (5); transposed y reads M, mu2, u1, lo1,
+#   ip1, writes mu1 (6); transposed x the same for mu0 (6); update reads gx, gy, gz, T, y0, y1, y2, mu0, mu1,
+#   mu2, lambda and the five accumulators and writes lambda and the accumulators (22)          -> 39 arrays
+# so one gradient evaluation moves (23 + 23 + 39) * 8 = 680 B and does about 25 + 25 + 51 = 101 FP64
+# operations per voxel and step.
+ADJ_BYTES_PER_VOXEL_STEP = (23 + 23 + 39) * 8
+ADJ_FP64_OPS_PER_VOXEL_STEP = 101
 
 
 def parse_args():
@@ -357,9 +368,10 @@ def adjoint_measurement(args, world, rank, dev):
     batched: 32 uneven two-phase instances (nz 24..48, ny,nx 96..192), 400 steps of 5 ms, checkpoint every 40,
     all in one concatenated state (one launch per sweep over every instance), against a loop of the
     single-instance adjoint over the same instances.  Device time from CUDA events around the steps."""
+    import ctypes
     import numpy as np
     import torch
-    from heatsim2_gb300 import workloads as W
+    from heatsim2_gb300 import _native, workloads as W
     from heatsim2_gb300.adjoint import Adjoint
     from heatsim2_gb300.batch import shard
 
@@ -373,11 +385,20 @@ def adjoint_measurement(args, world, rank, dev):
         a.backward()
     fwd, bwd = a.forward_ms, a.backward_ms
     vox = int(np.prod(w["shape"]))
+    hbm_peak, _ = read_peaks()
+    fma_rate = ctypes.c_double(0.0)
+    _native.check(_native.load().hs2g_fp64_fma_rate(torch.cuda.current_device(), ctypes.byref(fma_rate)))
+
+    def fracs(voxel_steps, ms):
+        return {"bytes_per_voxel_step": ADJ_BYTES_PER_VOXEL_STEP,
+                "fp64_ops_per_voxel_step": ADJ_FP64_OPS_PER_VOXEL_STEP,
+                "hbm_frac": ADJ_BYTES_PER_VOXEL_STEP * voxel_steps / (ms * 1e-3) / (hbm_peak * 1e9),
+                "fp64_frac": ADJ_FP64_OPS_PER_VOXEL_STEP * voxel_steps / (ms * 1e-3) / fma_rate.value}
     out["steel"] = {"workload": "steel (32,128,128) lognormal k, %d steps dt=10 ms, checkpoint %d"
                                 % (w["nsteps"], w["ckpt"]),
                     "gradient_evals_per_s": 1e3 / (fwd + bwd), "forward_ms": fwd, "backward_ms": bwd,
                     "forward_voxel_steps_per_s": vox * w["nsteps"] / (fwd * 1e-3),
-                    "device_bytes": a.device_bytes}
+                    "roofline": fracs(vox * w["nsteps"], fwd + bwd), "device_bytes": a.device_bytes}
     del a
     insts_all = W.adjoint_batch(**steps_kw)
     sizes = [int(np.prod(x["shape"])) for x in insts_all]
@@ -414,6 +435,8 @@ def adjoint_measurement(args, world, rank, dev):
     out["batched"] = {"workload": "%d uneven two-phase instances (nz 24..48, ny,nx 96..192), %d steps dt=5 ms, "
                                   "checkpoint %d" % (len(insts_all), insts[0]["nsteps"], insts[0]["ckpt"]),
                       "voxels": sum(sizes), "gradient_evals_per_s": batch_evals, "ms_per_eval_batch": batch_ms,
+                      "roofline": fracs(sum(int(np.prod(x["shape"])) for x in insts) * insts[0]["nsteps"],
+                                        batch_ms),
                       "device_bytes": bytes_b,
                       "single_loop": {"gradient_evals_per_s": loop_evals, "instances_timed": nloop,
                                       "max_rel_diff_vs_batch": worst},
