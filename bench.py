@@ -16,7 +16,7 @@ bandwidth; ``fp64_roofline`` the whole step against the measured FP64 FMA rate, 
 ``cpu_baseline`` the reference (or, where it cannot be built, the oracle) on the host cores.  ``batched`` is
 the 256-instance uneven batch (FP64 and FP32) against a per-instance loop of the plain path; ``adjoint`` the
 gradient evaluations per second of the (32,128,128) steel inverse problem and of the 32-instance batched
-adjoint against a loop of single-instance adjoints.
+adjoint against a loop of single-instance adjoints; ``curved`` the benchmark grid in the curved-surface mode.
 """
 import argparse
 import json
@@ -70,6 +70,7 @@ def parse_args():
     ap.add_argument("--batch-instances", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=100)
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-curved", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=None,
                     help="steps of both adjoint workloads (default: their own 500 and 400; smaller for profiling)")
     ap.add_argument("--adjoint-loop", type=int, default=32,
@@ -361,6 +362,43 @@ def batched_measurement(args, world, rank, dev):
     return out
 
 
+def curved_measurement(args, dev, steps=200):
+    """The reference's curved-surface mode (crank_nicolson.pyx:388-457) on the benchmark grid: the composite
+    panel under uniform surface curvatures of 2 /m along y and 1 /m along x (radii 0.5 m and 1 m), compiled
+    from per-row conductances (hs2g_create_rows); setup time and voxel-steps/s over ``steps`` steps."""
+    import ctypes
+    import numpy as np
+    import torch
+    import heatsim2_gb300 as hs
+    from heatsim2_gb300 import _native, workloads as W
+    from heatsim2_gb300.alternatingdirection import _ClassSources, source_table
+
+    L = _native.load()
+    spec = W.curved(workload(args.shape, steps), ky=2.0, kx=1.0)
+    t0 = time.perf_counter()
+    P, S = hs.setup(*W.setup_args(hs, spec), **W.setup_kwargs(spec))
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    src = _ClassSources(W.volumetric_tuple(hs, spec), True)
+    qtabs = np.ascontiguousarray([source_table(src, t, spec["dt"], P.volume_array)[0]
+                                  for t in W.step_times(spec, steps)])
+    T = torch.from_numpy(W.initial_temperature(spec)).to(dev)
+    stream = torch.cuda.Stream(device=dev)
+    _native.check(L.hs2g_set_stream(P.handle.ptr, ctypes.c_void_p(stream.cuda_stream)))
+    kms = np.zeros(4)
+    _native.check(L.hs2g_run_timed(P.handle.ptr, 3, T.data_ptr(), T.data_ptr(), qtabs.ctypes.data, _native.DEVICE,
+                                   kms.ctypes.data))
+    T.copy_(torch.from_numpy(W.initial_temperature(spec)))
+    torch.cuda.synchronize()
+    _native.check(L.hs2g_run_timed(P.handle.ptr, steps, T.data_ptr(), T.data_ptr(), qtabs.ctypes.data,
+                                   _native.DEVICE, kms.ctypes.data))
+    torch.cuda.synchronize()
+    return {"workload": "composite panel %dx%dx%d, surface curvatures 2 /m (y) and 1 /m (x), %d steps"
+                        % (tuple(args.shape) + (steps,)),
+            "value": spec["compute_voxels"] * steps / (float(kms[3]) * 1e-3), "unit": METRIC,
+            "ms_per_step": float(kms[3]) / steps, "setup_s": setup_s}
+
+
 def adjoint_measurement(args, world, rank, dev):
     """Gradient evaluations (forward pass + checkpointed backward pass) per second.
 
@@ -548,6 +586,10 @@ def gpu_arm(args, world, rank, local_rank):
         del P, S
         torch.cuda.empty_cache()
         batched = batched_measurement(args, world, rank, dev)
+    curved = None
+    if not args.no_curved:
+        torch.cuda.empty_cache()
+        curved = curved_measurement(args, dev)
     adjoint = None
     if not args.no_adjoint:
         torch.cuda.empty_cache()
@@ -572,7 +614,7 @@ def gpu_arm(args, world, rank, local_rank):
             "kernel_ms_per_step": per_kernel_ms, "kernel_fp64_frac": per_kernel_fp64,
             "kernel_hbm_frac": per_kernel_hbm,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * K, "clocks": clk, "setup_s": setup_s,
-            "device_bytes": state_bytes, "batched": batched, "adjoint": adjoint,
+            "device_bytes": state_bytes, "batched": batched, "adjoint": adjoint, "curved": curved,
         }
         print(json.dumps(line), flush=True)
 

@@ -31,7 +31,7 @@ EXPORTED = ("hs2g_abi_version", "hs2g_last_error", "hs2g_create_classes", "hs2g_
             "hs2g_batch_set_clock", "hs2g_batch_run", "hs2g_batch_autotune",
             "hs2g_adjoint_create", "hs2g_adjoint_destroy", "hs2g_adjoint_set_stream", "hs2g_adjoint_layout",
             "hs2g_adjoint_device_bytes", "hs2g_adjoint_set_parameters", "hs2g_adjoint_forward",
-            "hs2g_adjoint_backward")
+            "hs2g_adjoint_backward", "hs2g_create_rows")
 STATIC_MAX_VOXELS = 1 << 20
 
 
@@ -63,6 +63,12 @@ class ClassProblem(ctypes.Structure):
                 ("materials", ctypes.POINTER(Material)), ("forms", ctypes.POINTER(FaceForm)),
                 ("material", ctypes.c_void_p), ("boundary_z", ctypes.c_void_p), ("boundary_y", ctypes.c_void_p),
                 ("boundary_x", ctypes.c_void_p), ("volumetric", ctypes.c_void_p)]
+
+
+class RowsProblem(ctypes.Structure):
+    _fields_ = [("nz", ctypes.c_int64), ("ny", ctypes.c_int64), ("nx", ctypes.c_int64)] + \
+               [(n, ctypes.c_void_p) for n in ("zlo", "zhi", "ylo", "yhi", "xlo", "xhi", "capacity", "fixed",
+                                               "volumetric")]
 
 
 class AdjointGrid(ctypes.Structure):
@@ -103,6 +109,8 @@ def load():
         L.hs2g_create_classes.restype = i32
         L.hs2g_create_dense.argtypes = [ctypes.POINTER(DenseProblem), i32, ctypes.POINTER(vp)]
         L.hs2g_create_dense.restype = i32
+        L.hs2g_create_rows.argtypes = [ctypes.POINTER(RowsProblem), i32, ctypes.POINTER(vp)]
+        L.hs2g_create_rows.restype = i32
         L.hs2g_destroy.argtypes = [vp]
         L.hs2g_destroy.restype = None
         L.hs2g_set_stream.argtypes = [vp, vp]

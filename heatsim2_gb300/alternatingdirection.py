@@ -87,7 +87,9 @@ class adi_step(object):
 class _ClassSources(object):
     """The class-uniform sources of a ``volumetric`` tuple, packed for hs2g_source_table."""
 
-    def __init__(self, volumetric):
+    def __init__(self, volumetric, per_voxel_volume=False):
+        """per_voxel_volume: the problem's cells differ in volume (curved-surface mode), so point-joules sources
+        are evaluated per voxel (J / (V dt), pyx:309-313)."""
         n = len(volumetric)
         if n > _native.MAX_CLASSES:
             raise ValueError("at most 256 source classes")
@@ -101,7 +103,7 @@ class _ClassSources(object):
                 vals = [float(v) for v in src[1:]]
                 self.params[c, :len(vals)] = vals
             elif k == IMPULSE_POINT_SOURCE_JOULES:
-                if isinstance(src[2], numbers.Number):
+                if isinstance(src[2], numbers.Number) and not per_voxel_volume:
                     self.kind[c] = k
                     self.params[c, :2] = (float(src[1]), float(src[2]))
                 else:
@@ -125,7 +127,11 @@ def _dense_source(shape, volume, t, dt, volumetric_elements, dense):
             if t == src[1]:
                 if q is None:
                     q = np.zeros(shape)
-                q[volumetric_elements == idx] = src[2] / (volume * dt)
+                sel = volumetric_elements == idx
+                if np.ndim(volume) > 0:     # per-cell volumes (curved-surface mode)
+                    q[sel] = src[2] / (volume[sel] * dt)
+                else:
+                    q[sel] = src[2] / (volume * dt)
         else:
             (_, t_imp, direc, offset, zgrid, ddz, jpm2, length) = src
             if t == t_imp:
@@ -156,8 +162,10 @@ def source_table(sources, t, dt, volume):
     """(qtab ndarray[256], any_active) for the class-uniform sources at time t."""
     qtab = np.zeros(_native.MAX_CLASSES)
     L = _native.load()
+    # with per-cell volumes the point-joules sources are per voxel, so the table needs no volume
+    vol = float(volume) if np.ndim(volume) == 0 else 1.0
     active = _native.check(L.hs2g_source_table(sources.n, sources.kind.ctypes.data, sources.params.ctypes.data,
-                                               float(t), float(dt), float(volume), qtab.ctypes.data))
+                                               float(t), float(dt), vol, qtab.ctypes.data))
     return qtab, active > 0
 
 
@@ -189,7 +197,7 @@ def run_adi_steps(ADI_params, ADI_steps, t, dt, Tarray, volumetric_elements, vol
     """Advance ``Tarray`` by one timestep; returns a new array (numpy in, numpy out; CUDA tensor in, tensor out)."""
     P = ADI_params
     L = _native.load()
-    sources = _ClassSources(volumetric)
+    sources = _ClassSources(volumetric, np.ndim(P.volume_array) > 0)
     qtab, active = source_table(sources, t, dt, P.volume_array)
     ve = volumetric_elements
     qdense = _dense_source(P.shape, P.volume_array, t, dt, np.asarray(ve), sources.dense) if sources.dense else None
@@ -236,7 +244,7 @@ def run(ADI_params, Tarray, times, dt, volumetric_elements, volumetric, record_l
     step, shape (len(times), ny, nx))."""
     P = ADI_params
     L = _native.load()
-    sources = _ClassSources(volumetric)
+    sources = _ClassSources(volumetric, np.ndim(P.volume_array) > 0)
     nz, ny, nx = P.shape
     times = [float(t) for t in times]
     n = len(times)

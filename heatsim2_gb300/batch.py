@@ -43,6 +43,8 @@ class Batch(object):
         self.precision = precision
         self.device = current_device() if device is None else device
         self.problems = [ClassProblem(*p) for p in problems]
+        if any(p.curvature is not None for p in self.problems):
+            raise NotImplementedError("curved-surface problems are not provided in the batched form")
         n = len(self.problems)
         if n < 1:
             raise ValueError("empty batch")

@@ -197,8 +197,18 @@ class ClassProblem(object):
                  material_elements, boundary_z_elements, boundary_y_elements, boundary_x_elements,
                  volumetric_elements, top_surface_y_curvatures=None, top_surface_x_curvatures=None,
                  unaligned_anisotropic=False):
+        self.curvature = None
         if top_surface_y_curvatures is not None or top_surface_x_curvatures is not None:
-            raise NotImplementedError("the curved top-surface mode (crank_nicolson.pyx:388-457) is not provided")
+            # curved-surface mode (pyx:388-457): per-cell curvatures along y and x, zero where not given
+            curv = []
+            for c in (top_surface_y_curvatures, top_surface_x_curvatures):
+                c = np.zeros((int(ny), int(nx))) if c is None else np.asarray(c, dtype="d")
+                if c.shape != (int(ny), int(nx)):
+                    raise ValueError("surface curvatures must have shape (ny, nx) = %s" % ((int(ny), int(nx)),))
+                if not np.isfinite(c).all():
+                    raise ValueError("surface curvatures must be finite")
+                curv.append(np.ascontiguousarray(c))
+            self.curvature = tuple(curv)
         if unaligned_anisotropic:
             raise NotImplementedError("the unaligned-anisotropic ADI mode (alternatingdirection_c_pyx.pyx:511-564) "
                                       "is not provided")
@@ -221,6 +231,7 @@ class ClassProblem(object):
         self.vol = _u8_array(volumetric_elements, "volumetric_elements", (nz, ny, nx))
         self.mats = compile_materials(materials, dt)
         self.forms = compile_boundary_forms(boundaries, dz, dy, dx)
+        self.boundaries = boundaries
         self.struct = _native.ClassProblem(nz, ny, nx, len(materials), len(boundaries), self.mats, self.forms,
                                            self.mat.ctypes.data, self.bz.ctypes.data, self.by.ctypes.data,
                                            self.bx.ctypes.data, self.vol.ctypes.data)
@@ -241,8 +252,9 @@ def setup(z0, y0, x0, dz, dy, dx, nz, ny, nx, dt, materials, boundaries, volumet
           top_surface_y_curvatures=None, top_surface_x_curvatures=None, unaligned_anisotropic=False):
     """Compile the problem; returns ``(ADI_params, ADI_steps)`` for ``run_adi_steps``.
 
-    Arguments as in the reference (crank_nicolson.pyx:128-142).  The curved-surface mode and the
-    unaligned-anisotropic 15-stage mode are not provided (NotImplementedError)."""
+    Arguments as in the reference (crank_nicolson.pyx:128-142).  With surface curvatures the problem compiles
+    in the reference's curved-surface mode (heatsim2_gb300.curvature; ``ADI_params.volume_array`` is then the
+    per-cell volume).  The unaligned-anisotropic 15-stage mode is not provided (NotImplementedError)."""
     from .alternatingdirection import adi_params, adi_step
     cp = ClassProblem(z0, y0, x0, dz, dy, dx, nz, ny, nx, dt, materials, boundaries, volumetric, material_elements,
                       boundary_z_elements, boundary_y_elements, boundary_x_elements, volumetric_elements,
@@ -256,8 +268,22 @@ def setup(z0, y0, x0, dz, dy, dx, nz, ny, nx, dt, materials, boundaries, volumet
     if rc != _native.OK:
         raise_compile_error(rc)
     handle = _Handle(h, device)
+    volume = dz * dy * dx
+    if cp.curvature is not None:
+        # the class compile above validated the problem exactly as the flat mode does; the curved problem's
+        # rows weigh every face by its cell's own geometry and compile from per-row conductances
+        from . import curvature
+        r, volume = curvature.rows(cp, boundaries, *cp.curvature)
+        rp = _native.RowsProblem(nz, ny, nx, *[r[n].ctypes.data for n in ("zlo", "zhi", "ylo", "yhi", "xlo", "xhi",
+                                                                         "capacity", "fixed")],
+                                 cp.vol.ctypes.data)
+        h2 = ctypes.c_void_p()
+        rc = L.hs2g_create_rows(ctypes.byref(rp), device, ctypes.byref(h2))
+        if rc != _native.OK:
+            raise_compile_error(rc)
+        handle = _Handle(h2, device)
     vol = cp.vol
-    params = adi_params(shape=(nz, ny, nx), volume_array=dz * dy * dx, dt=dt, handle=handle, device=device,
+    params = adi_params(shape=(nz, ny, nx), volume_array=volume, dt=dt, handle=handle, device=device,
                         spacing=(dz, dy, dx), origin=(z0, y0, x0), compiled_volumetric=vol.copy())
     steps = tuple(adi_step(params, perm, s) for s, perm in enumerate(((0, 1, 2), (2, 0, 1), (1, 2, 0))))
     return params, steps

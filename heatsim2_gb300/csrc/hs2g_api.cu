@@ -49,6 +49,7 @@ struct hs2g_handle {
   unsigned long long* err_dev = nullptr;
   int* status_dev = nullptr;
   bool bulk_y = false, bulk_z = false;
+  bool per_row = false;  // compiled from per-row conductances (hs2g_create_rows): no shared face arrays
   hs2g::TensorMapCache* tmaps = nullptr;
   int64_t bytes = 0;
   // host-buffer steps overlap their copies with the sweeps: a copy stream, one stream per upload slab for
@@ -163,12 +164,12 @@ int check_kernel_error(hs2g_handle* h) {
               (long long)i);
 }
 
-int alloc_common(hs2g_handle* h) {
+int alloc_common(hs2g_handle* h, bool faces = true) {
   const int64_t n = h->d.nvox();
   int rc;
-  if ((rc = dalloc(h, &h->Gz, (h->d.nz + 1) * h->d.nxy(), "Gz"))) return rc;
-  if ((rc = dalloc(h, &h->Gy, h->d.nz * (h->d.ny + 1) * h->d.nx, "Gy"))) return rc;
-  if ((rc = dalloc(h, &h->Gx, h->d.nz * h->d.ny * (h->d.nx + 1), "Gx"))) return rc;
+  if (faces && (rc = dalloc(h, &h->Gz, (h->d.nz + 1) * h->d.nxy(), "Gz"))) return rc;
+  if (faces && (rc = dalloc(h, &h->Gy, h->d.nz * (h->d.ny + 1) * h->d.nx, "Gy"))) return rc;
+  if (faces && (rc = dalloc(h, &h->Gx, h->d.nz * h->d.ny * (h->d.nx + 1), "Gx"))) return rc;
   if ((rc = dalloc(h, &h->M, n, "capacity"))) return rc;
   if ((rc = dalloc(h, &h->compute, n, "compute mask"))) return rc;
   if ((rc = dalloc(h, &h->vclass, n, "source classes"))) return rc;
@@ -502,6 +503,72 @@ int hs2g_create_dense(const hs2g_dense_problem* p, int device, hs2g_handle** out
   return HS2G_OK;
 }
 
+int hs2g_create_rows(const hs2g_rows_problem* p, int device, hs2g_handle** out) {
+  if (!p || !out) return fail(HS2G_ERR_ARG, "null argument");
+  *out = nullptr;
+  const double* src[6] = {p->zlo, p->zhi, p->ylo, p->yhi, p->xlo, p->xhi};
+  for (const double* a : src)
+    if (!a) return fail(HS2G_ERR_ARG, "null array in problem");
+  if (!p->capacity) return fail(HS2G_ERR_ARG, "null array in problem");
+  DeviceGuard g(device);
+  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", device);
+  hs2g_handle* h = nullptr;
+  int rc = new_handle(device, Dims{p->nz, p->ny, p->nx}, &h);
+  if (rc) return rc;
+  const Dims& d = h->d;
+  const int64_t n = d.nvox();
+  double* rows = nullptr;  // the six per-row arrays live on the device only while the problem is compiled
+  auto bail = [&](int code) {
+    std::string msg = g_last_error;
+    if (rows) dfree(h, rows, 6 * n);
+    hs2g_destroy(h);
+    g_last_error = msg;
+    return code;
+  };
+  h->per_row = true;
+  if ((rc = alloc_common(h, false))) return bail(rc);
+  if ((rc = dalloc(h, &rows, 6 * n, "per-row conductances"))) return bail(rc);
+  cudaStream_t s = h->stream;
+  cudaError_t e = cudaSuccess;
+  auto up = [&](void* dst, const void* from, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dst, from, bytes, cudaMemcpyHostToDevice, s);
+  };
+  const double* dev_rows[6];
+  for (int r = 0; r < 6; ++r) {
+    dev_rows[r] = rows + (int64_t)r * n;
+    up(rows + (int64_t)r * n, src[r], sizeof(double) * n);
+  }
+  up(h->M, p->capacity, sizeof(double) * n);
+  std::vector<uint8_t> comp((size_t)n, 1);
+  if (p->fixed)
+    for (int64_t v = 0; v < n; ++v) comp[(size_t)v] = p->fixed[v] ? 0 : 1;
+  up(h->compute, comp.data(), (size_t)n);
+  if (p->volumetric)
+    up(h->vclass, p->volumetric, (size_t)n);
+  else if (e == cudaSuccess)
+    e = cudaMemsetAsync(h->vclass, 0, (size_t)n, s);
+  if (e == cudaSuccess) e = hs2g::launch_validate_rows(d, dev_rows, h->M, h->compute, h->err_dev, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  rc = (e != cudaSuccess) ? cuda_fail(e, "per-row compile") : check_kernel_error(h);
+  if (rc) return bail(rc);
+  double *s2 = nullptr, *sigma = nullptr;
+  if ((rc = dalloc(h, &s2, n, "factor scratch"))) return bail(rc);
+  if ((rc = dalloc(h, &sigma, n, "factor scratch"))) {
+    dfree(h, s2, n);
+    return bail(rc);
+  }
+  e = hs2g::launch_factor_rows(d, dev_rows, h->M, h->compute, s2, sigma, h->c, s);
+  cudaError_t e2 = cudaStreamSynchronize(s);
+  dfree(h, s2, n);
+  dfree(h, sigma, n);
+  dfree(h, rows, 6 * n);
+  rows = nullptr;
+  if (e != cudaSuccess) return bail(cuda_fail(e, "factor kernels"));
+  if (e2 != cudaSuccess) return bail(cuda_fail(e2, "factor kernels"));
+  *out = h;
+  return HS2G_OK;
+}
+
 int hs2g_set_stream(hs2g_handle* h, void* stream) {
   if (!h) return fail(HS2G_ERR_ARG, "null handle");
   h->stream = (cudaStream_t)stream;
@@ -744,6 +811,8 @@ int hs2g_fp64_fma_rate(int device, double* fma_per_s) {
 
 int hs2g_get_faces(hs2g_handle* h, double* Gz, double* Gy, double* Gx, double* capacity, uint8_t* fixed) {
   if (!h) return fail(HS2G_ERR_ARG, "null handle");
+  if (h->per_row && (Gz || Gy || Gx))
+    return fail(HS2G_ERR_STATE, "a per-row problem has no shared face conductances");
   DeviceGuard g(h->device);
   const Dims& d = h->d;
   const int64_t n = d.nvox();

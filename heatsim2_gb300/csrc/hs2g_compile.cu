@@ -155,17 +155,49 @@ __device__ __forceinline__ RowIn stage_row(bool comp, double M, double gl, doubl
   return r;
 }
 
+// The six face conductances of voxel p as its own row sees them.  SharedFaces: one array per axis indexed by
+// face, so the two rows of a face see the same value (the class and dense problems).  RowFaces: six
+// (nz, ny, nx) arrays, one value per row and side, so a face may weigh differently in its two rows (the
+// reference's curved-surface mode, where each row uses its own cell's edge lengths).
+struct SharedFaces {
+  const double *Gz, *Gy, *Gx;
+  __device__ double zlo(const Dims& d, int64_t p, int64_t, int64_t, int64_t) const { return Gz[p]; }
+  __device__ double zhi(const Dims& d, int64_t p, int64_t, int64_t, int64_t) const { return Gz[p + d.nxy()]; }
+  __device__ double ylo(const Dims& d, int64_t, int64_t k, int64_t j, int64_t i) const {
+    return Gy[(k * (d.ny + 1) + j) * d.nx + i];
+  }
+  __device__ double yhi(const Dims& d, int64_t, int64_t k, int64_t j, int64_t i) const {
+    return Gy[(k * (d.ny + 1) + j + 1) * d.nx + i];
+  }
+  __device__ double xlo(const Dims& d, int64_t, int64_t k, int64_t j, int64_t i) const {
+    return Gx[(k * d.ny + j) * (d.nx + 1) + i];
+  }
+  __device__ double xhi(const Dims& d, int64_t, int64_t k, int64_t j, int64_t i) const {
+    return Gx[(k * d.ny + j) * (d.nx + 1) + i + 1];
+  }
+};
+struct RowFaces {
+  const double *zl, *zh, *yl, *yh, *xl, *xh;
+  __device__ double zlo(const Dims&, int64_t p, int64_t, int64_t, int64_t) const { return zl[p]; }
+  __device__ double zhi(const Dims&, int64_t p, int64_t, int64_t, int64_t) const { return zh[p]; }
+  __device__ double ylo(const Dims&, int64_t p, int64_t, int64_t, int64_t) const { return yl[p]; }
+  __device__ double yhi(const Dims&, int64_t p, int64_t, int64_t, int64_t) const { return yh[p]; }
+  __device__ double xlo(const Dims&, int64_t p, int64_t, int64_t, int64_t) const { return xl[p]; }
+  __device__ double xhi(const Dims&, int64_t p, int64_t, int64_t, int64_t) const { return xh[p]; }
+};
+
 // z lines (one thread per (j,i)): stage-2 coefficients and s2.
-__global__ void factor_z_kernel(Dims d, const double* __restrict__ Gz, const double* __restrict__ M,
-                                const uint8_t* __restrict__ compute, double* __restrict__ s2,
-                                double* __restrict__ a2, double* __restrict__ b2) {
+template <class F>
+__global__ void factor_z_kernel(Dims d, F g, const double* __restrict__ M, const uint8_t* __restrict__ compute,
+                                double* __restrict__ s2, double* __restrict__ a2, double* __restrict__ b2) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= d.nxy()) return;
+  const int64_t j = t / d.nx, i = t - j * d.nx;
   double u_prev = 0.0;
   for (int64_t k = 0; k < d.nz; ++k) {
     const int64_t p = k * d.nxy() + t;
     const bool comp = compute[p] != 0;
-    const RowIn r = stage_row(comp, M[p], comp ? Gz[p] : 0.0, comp ? Gz[p + d.nxy()] : 0.0);
+    const RowIn r = stage_row(comp, M[p], comp ? g.zlo(d, p, k, j, i) : 0.0, comp ? g.zhi(d, p, k, j, i) : 0.0);
     const double piv = r.d - u_prev * r.lo;
     const double u = r.hi / piv;
     a2[p] = r.lo / piv;
@@ -176,18 +208,18 @@ __global__ void factor_z_kernel(Dims d, const double* __restrict__ Gz, const dou
 }
 
 // y lines (one thread per (k,i)): stage-1 coefficients and sigma.
-__global__ void factor_y_kernel(Dims d, const double* __restrict__ Gy, const double* __restrict__ M,
-                                const uint8_t* __restrict__ compute, const double* __restrict__ s2,
-                                double* __restrict__ sigma, double* __restrict__ a1, double* __restrict__ b1) {
+template <class F>
+__global__ void factor_y_kernel(Dims d, F g, const double* __restrict__ M, const uint8_t* __restrict__ compute,
+                                const double* __restrict__ s2, double* __restrict__ sigma, double* __restrict__ a1,
+                                double* __restrict__ b1) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= d.nz * d.nx) return;
   const int64_t k = t / d.nx, i = t - k * d.nx;
   double u_prev = 0.0, s2_prev = 1.0;
   for (int64_t j = 0; j < d.ny; ++j) {
     const int64_t p = (k * d.ny + j) * d.nx + i;
-    const int64_t f = (k * (d.ny + 1) + j) * d.nx + i;
     const bool comp = compute[p] != 0;
-    const RowIn r = stage_row(comp, M[p], comp ? Gy[f] : 0.0, comp ? Gy[f + d.nx] : 0.0);
+    const RowIn r = stage_row(comp, M[p], comp ? g.ylo(d, p, k, j, i) : 0.0, comp ? g.yhi(d, p, k, j, i) : 0.0);
     const double piv = r.d - u_prev * r.lo;
     const double u = r.hi / piv;
     const double s2p = s2[p];
@@ -200,9 +232,9 @@ __global__ void factor_y_kernel(Dims d, const double* __restrict__ Gy, const dou
 }
 
 // x lines (one thread per (k,j)): stage-0 stencil, forward and back coefficients.
-__global__ void factor_x_kernel(Dims d, const double* __restrict__ Gz, const double* __restrict__ Gy,
-                                const double* __restrict__ Gx, const double* __restrict__ M,
-                                const uint8_t* __restrict__ compute, const double* __restrict__ sigma, Coeffs c) {
+template <class F>
+__global__ void factor_x_kernel(Dims d, F g, const double* __restrict__ M, const uint8_t* __restrict__ compute,
+                                const double* __restrict__ sigma, Coeffs c) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= d.nz * d.ny) return;
   const int64_t k = t / d.ny, j = t - k * d.ny;
@@ -210,11 +242,9 @@ __global__ void factor_x_kernel(Dims d, const double* __restrict__ Gz, const dou
   for (int64_t i = 0; i < d.nx; ++i) {
     const int64_t p = t * d.nx + i;
     const bool comp = compute[p] != 0;
-    const int64_t fx = t * (d.nx + 1) + i;
-    const int64_t fy = (k * (d.ny + 1) + j) * d.nx + i;
-    const double gxl = comp ? Gx[fx] : 0.0, gxh = comp ? Gx[fx + 1] : 0.0;
-    const double gyl = comp ? Gy[fy] : 0.0, gyh = comp ? Gy[fy + d.nx] : 0.0;
-    const double gzl = comp ? Gz[p] : 0.0, gzh = comp ? Gz[p + d.nxy()] : 0.0;
+    const double gxl = comp ? g.xlo(d, p, k, j, i) : 0.0, gxh = comp ? g.xhi(d, p, k, j, i) : 0.0;
+    const double gyl = comp ? g.ylo(d, p, k, j, i) : 0.0, gyh = comp ? g.yhi(d, p, k, j, i) : 0.0;
+    const double gzl = comp ? g.zlo(d, p, k, j, i) : 0.0, gzh = comp ? g.zhi(d, p, k, j, i) : 0.0;
     const RowIn r = stage_row(comp, M[p], gxl, gxh);
     const double piv = r.d - u_prev * r.lo;
     const double u = r.hi / piv;
@@ -236,6 +266,27 @@ __global__ void factor_x_kernel(Dims d, const double* __restrict__ Gz, const dou
     c.b0[p] = b0;
     u_prev = u;
     sg_prev = sg;
+  }
+}
+
+// per-row problem: capacities positive and finite, coefficients finite, exterior sides zero on computed
+// voxels (the same rules as validate_dense_kernel); fixed voxels get the unit capacity of an identity row
+__global__ void validate_rows_kernel(Dims d, RowFaces g, double* __restrict__ M, uint8_t* __restrict__ compute,
+                                     unsigned long long* err) {
+  const int64_t n = d.nvox();
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = p % d.nx, j = (p / d.nx) % d.ny, k = p / d.nxy();
+    if (!compute[p]) {
+      M[p] = 1.0;
+      continue;
+    }
+    const double cap = M[p];
+    if (!(cap > 0.0 && cap < INFINITY)) record_error(err, HS2G_ERR_CAPACITY, 3, p);
+    if ((k == 0 && g.zl[p] != 0.0) || (k == d.nz - 1 && g.zh[p] != 0.0)) record_error(err, HS2G_ERR_EXTERIOR, 0, p);
+    if ((j == 0 && g.yl[p] != 0.0) || (j == d.ny - 1 && g.yh[p] != 0.0)) record_error(err, HS2G_ERR_EXTERIOR, 1, p);
+    if ((i == 0 && g.xl[p] != 0.0) || (i == d.nx - 1 && g.xh[p] != 0.0)) record_error(err, HS2G_ERR_EXTERIOR, 2, p);
+    const double all = g.zl[p] + g.zh[p] + g.yl[p] + g.yh[p] + g.xl[p] + g.xh[p];
+    if (!(all == all) || isinf(all)) record_error(err, HS2G_ERR_ARG, 3, p);
   }
 }
 
@@ -270,12 +321,31 @@ cudaError_t launch_validate_dense(const Dims& d, const double* Gz, const double*
   return cudaGetLastError();
 }
 
+template <class F>
+cudaError_t launch_factor_with(const Dims& d, F g, const double* M, const uint8_t* compute, double* s2,
+                               double* sigma, const Coeffs& c, cudaStream_t s) {
+  const int th = 128;
+  factor_z_kernel<F><<<grid_for(d.nxy(), th), th, 0, s>>>(d, g, M, compute, s2, c.a2, c.b2);
+  factor_y_kernel<F><<<grid_for(d.nz * d.nx, th), th, 0, s>>>(d, g, M, compute, s2, sigma, c.a1, c.b1);
+  factor_x_kernel<F><<<grid_for(d.nz * d.ny, th), th, 0, s>>>(d, g, M, compute, sigma, c);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_factor(const Dims& d, const double* Gz, const double* Gy, const double* Gx, const double* M,
                           const uint8_t* compute, double* s2, double* sigma, const Coeffs& c, cudaStream_t s) {
-  const int th = 128;
-  factor_z_kernel<<<grid_for(d.nxy(), th), th, 0, s>>>(d, Gz, M, compute, s2, c.a2, c.b2);
-  factor_y_kernel<<<grid_for(d.nz * d.nx, th), th, 0, s>>>(d, Gy, M, compute, s2, sigma, c.a1, c.b1);
-  factor_x_kernel<<<grid_for(d.nz * d.ny, th), th, 0, s>>>(d, Gz, Gy, Gx, M, compute, sigma, c);
+  return launch_factor_with(d, SharedFaces{Gz, Gy, Gx}, M, compute, s2, sigma, c, s);
+}
+
+cudaError_t launch_factor_rows(const Dims& d, const double* const rows[6], const double* M, const uint8_t* compute,
+                               double* s2, double* sigma, const Coeffs& c, cudaStream_t s) {
+  const RowFaces g{rows[0], rows[1], rows[2], rows[3], rows[4], rows[5]};
+  return launch_factor_with(d, g, M, compute, s2, sigma, c, s);
+}
+
+cudaError_t launch_validate_rows(const Dims& d, const double* const rows[6], double* M, uint8_t* compute,
+                                 unsigned long long* err, cudaStream_t s) {
+  const RowFaces g{rows[0], rows[1], rows[2], rows[3], rows[4], rows[5]};
+  validate_rows_kernel<<<grid_for(d.nvox(), kThreads), kThreads, 0, s>>>(d, g, M, compute, err);
   return cudaGetLastError();
 }
 

@@ -62,6 +62,11 @@ cudaError_t launch_validate_dense(const Dims& d, const double* Gz, const double*
                                   double* M, uint8_t* compute, unsigned long long* err, cudaStream_t s);
 cudaError_t launch_factor(const Dims& d, const double* Gz, const double* Gy, const double* Gx, const double* M,
                           const uint8_t* compute, double* s2, double* sigma, const Coeffs& c, cudaStream_t s);
+// per-row problems: rows = {z lo, z hi, y lo, y hi, x lo, x hi}, each (nz, ny, nx)
+cudaError_t launch_validate_rows(const Dims& d, const double* const rows[6], double* M, uint8_t* compute,
+                                 unsigned long long* err, cudaStream_t s);
+cudaError_t launch_factor_rows(const Dims& d, const double* const rows[6], const double* M, const uint8_t* compute,
+                               double* s2, double* sigma, const Coeffs& c, cudaStream_t s);
 
 // step kernels (hs2g_sweep.cu)
 struct StepArgs {

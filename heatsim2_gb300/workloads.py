@@ -87,6 +87,28 @@ def setup_args(hs, spec):
             a["material"], a["boundary_z"], a["boundary_y"], a["boundary_x"], a["volumetric"])
 
 
+def setup_kwargs(spec):
+    """Keyword arguments of ``hs.setup`` for this spec: the surface curvatures of a curved spec, else none."""
+    a = spec.get("arrays", {})
+    if "curv_y" in a or "curv_x" in a:
+        return {"top_surface_y_curvatures": a.get("curv_y"), "top_surface_x_curvatures": a.get("curv_x")}
+    return {}
+
+
+def curved(spec, seed=0, ky=None, kx=None, amplitude=20.0):
+    """A copy of ``spec`` in the reference's curved-surface mode: curvatures (1/m, positive concave) along y and
+    x per surface cell, given or seeded uniform in [-amplitude, amplitude]."""
+    g = spec["grid"]
+    rng = np.random.default_rng(seed)
+    shape = (g["ny"], g["nx"])
+    ky = rng.uniform(-amplitude, amplitude, shape) if ky is None else np.broadcast_to(ky, shape).astype("d")
+    kx = rng.uniform(-amplitude, amplitude, shape) if kx is None else np.broadcast_to(kx, shape).astype("d")
+    out = dict(spec)
+    out["name"] = "curved_" + spec["name"]
+    out["arrays"] = dict(spec["arrays"], curv_y=np.ascontiguousarray(ky), curv_x=np.ascontiguousarray(kx))
+    return out
+
+
 def initial_temperature(spec):
     g = spec["grid"]
     return np.full((g["nz"], g["ny"], g["nx"]), float(spec.get("T0", T_AMBIENT)), dtype="d")

@@ -110,6 +110,24 @@ typedef struct {
   const uint8_t* volumetric;        /* (nz, ny, nx) source classes, or NULL for class 0 everywhere */
 } hs2g_dense_problem;
 
+/* Problem described by per-row face conductances: for every voxel, the conductance of each of its six faces
+   as that voxel's own heat balance weighs it (W/m^3/K), so the two rows of a face may differ.  This is the
+   reference's curved-surface mode (crank_nicolson.pyx:388-457) after each row is divided by its cell volume:
+   face areas and edge lengths follow the cell's depth and the surface curvature.  Exterior sides of computed
+   voxels must be zero. */
+typedef struct {
+  int64_t nz, ny, nx;
+  const double* zlo;                /* (nz, ny, nx) each: the low and high face of every voxel on z, y, x */
+  const double* zhi;
+  const double* ylo;
+  const double* yhi;
+  const double* xlo;
+  const double* xhi;
+  const double* capacity;           /* (nz, ny, nx) rho*c/dt */
+  const uint8_t* fixed;             /* (nz, ny, nx) 1 = fixed temperature, or NULL for none */
+  const uint8_t* volumetric;        /* (nz, ny, nx) source classes, or NULL for class 0 everywhere */
+} hs2g_rows_problem;
+
 typedef struct hs2g_handle hs2g_handle;
 
 int hs2g_abi_version(void);
@@ -120,6 +138,7 @@ const char* hs2g_last_error(void);
    alternatingdirection_c_pyx.pyx:212-282 finalize, tridiag.pyx:9-43 tridiaglu). */
 int hs2g_create_classes(const hs2g_class_problem* problem, int device, hs2g_handle** out);
 int hs2g_create_dense(const hs2g_dense_problem* problem, int device, hs2g_handle** out);
+int hs2g_create_rows(const hs2g_rows_problem* problem, int device, hs2g_handle** out);
 /* Free every device buffer of the handle (replaces delete_adi_step, alternatingdirection_c.c:14-54). */
 void hs2g_destroy(hs2g_handle* h);
 
@@ -254,7 +273,8 @@ int hs2g_adjoint_forward(hs2g_adjoint* a, int nsteps, const double* schedule, co
 int hs2g_adjoint_backward(hs2g_adjoint* a, double* gk, double* gC, double* gq, double* gT0, int flags,
                           double* elapsed_ms);
 
-/* Copy the compiled face conductances and capacities to host buffers (any may be NULL). */
+/* Copy the compiled face conductances and capacities to host buffers (any may be NULL).  A handle made by
+   hs2g_create_rows has no shared face conductances: asking for Gz, Gy or Gx returns HS2G_ERR_STATE. */
 int hs2g_get_faces(hs2g_handle* h, double* Gz, double* Gy, double* Gx, double* capacity, uint8_t* fixed);
 
 /* Device bytes held by the handle. */

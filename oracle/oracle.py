@@ -170,7 +170,11 @@ def source_field(shape, volume, t, dt, volumetric_elements, volumetric):
                 q[volumetric_elements == idx] = src[3]
         elif kind == IMPULSE_POINT_SOURCE_JOULES:
             if t == src[1]:
-                q[volumetric_elements == idx] = src[2] / (volume * dt)
+                sel = volumetric_elements == idx
+                if np.ndim(volume) > 0:     # per-cell volumes, curved-surface mode (:309-313)
+                    q[sel] = src[2] / (volume[sel] * dt)
+                else:
+                    q[sel] = src[2] / (volume * dt)
         elif kind == SPATIALLY_Z_DECAYING_TEMPORAL_IMPULSE:
             (_, t_imp, direc, offset, zgrid, ddz, jpm2, length) = src
             if t == t_imp:

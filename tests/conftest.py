@@ -17,11 +17,14 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "slow: long-running")
 
 
-def golden_files(include_big=True):
+def golden_files(include_big=True, curved=False):
+    """The reference's output fixtures: flat problems, or (curved=True) those in the curved-surface mode."""
     out = []
     for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
         b = os.path.basename(f)
         if b.startswith("stages_") or b == "tridiag.npz":
+            continue
+        if b.startswith("curved_") != curved:
             continue
         out.append(f)
     return out

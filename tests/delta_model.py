@@ -53,6 +53,12 @@ def faces_from_classes(shape, materials, boundaries, dz, dy, dx, dt, mat, bz, by
 
 
 def factor(Gz, Gy, Gx, M, comp):
+    """Coefficients from shared face conductances (class and dense problems)."""
+    return factor_rows(Gz[:-1], Gz[1:], Gy[:, :-1], Gy[:, 1:], Gx[:, :, :-1], Gx[:, :, 1:], M, comp)
+
+
+def factor_rows(gzl, gzh, gyl, gyh, gxl, gxh, M, comp):
+    """Coefficients from per-row face conductances (hs2g_compile.cu factor kernels with RowFaces)."""
     nz, ny, nx = M.shape
     c = {}
 
@@ -63,9 +69,7 @@ def factor(Gz, Gy, Gx, M, comp):
         return d, lo, hi
 
     z = lambda a: np.where(comp, a, 0.0)
-    gzl, gzh = z(Gz[:-1]), z(Gz[1:])
-    gyl, gyh = z(Gy[:, :-1]), z(Gy[:, 1:])
-    gxl, gxh = z(Gx[:, :, :-1]), z(Gx[:, :, 1:])
+    gzl, gzh, gyl, gyh, gxl, gxh = (z(a) for a in (gzl, gzh, gyl, gyh, gxl, gxh))
     # z lines
     d, lo, hi = row(gzl, gzh)
     a2 = np.zeros_like(M); b2 = np.zeros_like(M); s2 = np.zeros_like(M)

@@ -3,7 +3,7 @@
 Run in a container where the reference sources are mounted (the reference is built into oracle/_ref by
 oracle/build_ref.py first):
 
-    python oracle/build_ref.py && python tests/golden/make_golden.py
+    python oracle/build_ref.py && python tests/golden/make_golden.py [curved]
 
 Each fixture ``<name>.npz`` holds the problem spec (heatsim2_gb300.workloads serialisation), the t values
 passed to the reference's run_adi_steps, and the temperature field the reference returned after selected
@@ -33,7 +33,7 @@ def quiet(fn, *a, **k):
 
 
 def run_reference(hs, spec, save_steps):
-    P, S = quiet(hs.setup, *W.setup_args(hs, spec))
+    P, S = quiet(hs.setup, *W.setup_args(hs, spec), **W.setup_kwargs(spec))
     vol = W.volumetric_tuple(hs, spec)
     T = W.initial_temperature(spec)
     times = W.step_times(spec)
@@ -84,10 +84,20 @@ def tridiag_fixture(hs_tridiag):
     print("wrote tridiag")
 
 
+def curved_fixtures(hs):
+    """The reference's curved-surface mode (crank_nicolson.pyx:388-457)."""
+    save_fixture("curved_mixed_small", W.curved(W.mixed_small(), seed=21), set(range(1, 7)), hs)
+    save_fixture("curved_sources_small", W.curved(W.sources_small(), ky=15.0, kx=-10.0), set(range(1, 6)), hs)
+    save_fixture("curved_steel_slab", W.curved(W.steel_slab(nsteps=20), seed=22, amplitude=8.0), {1, 5, 20}, hs)
+
+
 def main():
     if not build_ref.available():
         build_ref.build()
     hs = build_ref.import_reference()
+    if len(sys.argv) > 1 and sys.argv[1] == "curved":
+        curved_fixtures(hs)
+        return
     import heatsim2.tridiag as ref_tridiag
     tridiag_fixture(ref_tridiag)
 
@@ -100,6 +110,7 @@ def main():
     save_fixture("sources_small", W.sources_small(), set(range(1, 6)), hs, stages=True)
     for shape in ((1, 1, 7), (7, 1, 1), (1, 7, 1), (1, 1, 1), (1, 5, 6), (4, 1, 5), (3, 4, 1)):
         save_fixture("line_%dx%dx%d" % shape, W.line_grid(shape), set(range(1, 6)), hs)
+    curved_fixtures(hs)
 
 
 if __name__ == "__main__":
