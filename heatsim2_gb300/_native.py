@@ -31,7 +31,7 @@ EXPORTED = ("hs2g_abi_version", "hs2g_last_error", "hs2g_create_classes", "hs2g_
             "hs2g_batch_set_clock", "hs2g_batch_run", "hs2g_batch_autotune",
             "hs2g_adjoint_create", "hs2g_adjoint_destroy", "hs2g_adjoint_set_stream", "hs2g_adjoint_layout",
             "hs2g_adjoint_device_bytes", "hs2g_adjoint_set_parameters", "hs2g_adjoint_forward",
-            "hs2g_adjoint_backward", "hs2g_create_rows")
+            "hs2g_adjoint_backward", "hs2g_create_rows", "hs2g_selftest_wait")
 STATIC_MAX_VOXELS = 1 << 20
 
 
@@ -111,6 +111,8 @@ def load():
         L.hs2g_create_dense.restype = i32
         L.hs2g_create_rows.argtypes = [ctypes.POINTER(RowsProblem), i32, ctypes.POINTER(vp)]
         L.hs2g_create_rows.restype = i32
+        L.hs2g_selftest_wait.argtypes = [i32, i64, i32, ctypes.POINTER(ctypes.c_int)]
+        L.hs2g_selftest_wait.restype = i32
         L.hs2g_destroy.argtypes = [vp]
         L.hs2g_destroy.restype = None
         L.hs2g_set_stream.argtypes = [vp, vp]

@@ -587,6 +587,7 @@ using hs2g::nblk;
 
 int afail(int code, const char* m) { return hs2g::set_last_error(code, m); }
 int acuda(cudaError_t e, const char* what) {
+  cudaGetLastError();  // a failed allocation leaves its error as the last error: clear it for later checks
   char buf[256];
   snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
   return hs2g::set_last_error(e == cudaErrorMemoryAllocation ? HS2G_ERR_NOMEM : HS2G_ERR_CUDA, buf);

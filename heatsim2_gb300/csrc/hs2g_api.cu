@@ -569,6 +569,20 @@ int hs2g_create_rows(const hs2g_rows_problem* p, int device, hs2g_handle** out) 
   return HS2G_OK;
 }
 
+int hs2g_selftest_wait(int device, int64_t limit_ns, int arrive, int* status) {
+  if (!status || limit_ns <= 0 || limit_ns > 10000000000ll)
+    return fail(HS2G_ERR_ARG, "hs2g_selftest_wait: limit must be in (0, 10 s]");
+  DeviceGuard g(device);
+  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", device);
+  int* st = nullptr;
+  cudaError_t e = cudaMalloc(&st, sizeof(int));
+  if (e != cudaSuccess) return cuda_fail(e, "hs2g_selftest_wait");
+  e = hs2g::wait_selftest((uint64_t)limit_ns, arrive, st, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(status, st, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(st);
+  return e == cudaSuccess ? HS2G_OK : cuda_fail(e, "hs2g_selftest_wait");
+}
+
 int hs2g_set_stream(hs2g_handle* h, void* stream) {
   if (!h) return fail(HS2G_ERR_ARG, "null handle");
   h->stream = (cudaStream_t)stream;

@@ -538,9 +538,10 @@ struct BatchDeviceGuard {
 
 int bfail(int code, const char* msg) { return hs2g::set_last_error(code, msg); }
 int bcuda(cudaError_t e, const char* what) {
+  cudaGetLastError();  // a failed allocation leaves its error as the last error: clear it for later checks
   char buf[256];
   snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
-  return hs2g::set_last_error(HS2G_ERR_CUDA, buf);
+  return hs2g::set_last_error(e == cudaErrorMemoryAllocation ? HS2G_ERR_NOMEM : HS2G_ERR_CUDA, buf);
 }
 
 template <typename T>

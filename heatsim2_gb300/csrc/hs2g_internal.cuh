@@ -98,6 +98,8 @@ cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable&
                                cudaEvent_t ev[4]);
 cudaError_t fp64_fma_rate(double* fma_per_s);
 cudaError_t launch_copy_layer(const Dims& d, const double* T, int layer, double* dst, cudaStream_t s);
+// one bounded mbarrier wait on a barrier that receives its arrival (arrive != 0) or none (hs2g_lines.cu)
+cudaError_t wait_selftest(uint64_t limit_ns, int arrive, int* status_dev, cudaStream_t s);
 // the step in pieces, for overlapping host copies with it: the x sweep over x-lines [line_begin, line_end)
 // (line = k*ny + j), the whole y sweep, the plain z sweep over columns [col_begin, col_end) (col = j*nx + i)
 cudaError_t launch_x_range(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_begin,

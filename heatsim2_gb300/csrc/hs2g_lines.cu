@@ -60,13 +60,29 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns = kWaitNs) {
   if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t deadline = now_ns() + kWaitNs;
+  const uint64_t deadline = now_ns() + limit_ns;
   while (!mbar_try_wait(bar, parity))
     if (now_ns() > deadline) return false;
   return true;
 }
+// Self-test of the bounded wait: one thread waits, for at most limit_ns, on an mbarrier that expects one
+// arrival, which it makes itself (arrive != 0) or which never comes.  A wait that gives up reports
+// HS2G_ERR_TIMEOUT through the status word, as a sweep whose copies never complete does; nothing is in
+// flight, so the kernel ends cleanly either way.
+__global__ void wait_selftest_kernel(uint64_t limit_ns, int arrive, int* status) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  if (arrive) mbar_arrive(&bar);
+  *status = mbar_wait_bounded(&bar, 0, limit_ns) ? HS2G_OK : HS2G_ERR_TIMEOUT;
+}
+
 // 3-D tile load (x = line index within the row, y = row, z = plane); coordinates may lie outside the array.
 __device__ __forceinline__ void tile_load(void* dst, const CUtensorMap* map, int c0, int c1, int c2, uint64_t* bar) {
   asm volatile(
@@ -325,6 +341,12 @@ cudaError_t launch_lines_bulk(const Dims& d, int axis, const double* A, const do
     line_sweep_tma_kernel<true><<<(unsigned)g.groups, kNL, smem_bytes<true>(), s>>>(g, mA, mAl, mS, mB, mT,
                                                                                     scratch, out, status);
   }
+  return cudaGetLastError();
+}
+
+
+cudaError_t wait_selftest(uint64_t limit_ns, int arrive, int* status_dev, cudaStream_t s) {
+  wait_selftest_kernel<<<1, 32, 0, s>>>(limit_ns, arrive, status_dev);
   return cudaGetLastError();
 }
 

@@ -273,6 +273,12 @@ int hs2g_adjoint_forward(hs2g_adjoint* a, int nsteps, const double* schedule, co
 int hs2g_adjoint_backward(hs2g_adjoint* a, double* gk, double* gC, double* gq, double* gT0, int flags,
                           double* elapsed_ms);
 
+/* Self-test of the bounded waits inside the TMA sweeps (failure detection without a fault): one thread waits
+   at most limit_ns (<= 10 s) on an mbarrier that receives its one arrival (arrive != 0) or none.  *status
+   receives HS2G_OK, or HS2G_ERR_TIMEOUT -- the status a sweep reports when its copies never complete -- and
+   the device stays usable either way. */
+int hs2g_selftest_wait(int device, int64_t limit_ns, int arrive, int* status);
+
 /* Copy the compiled face conductances and capacities to host buffers (any may be NULL).  A handle made by
    hs2g_create_rows has no shared face conductances: asking for Gz, Gy or Gx returns HS2G_ERR_STATE. */
 int hs2g_get_faces(hs2g_handle* h, double* Gz, double* Gy, double* Gx, double* capacity, uint8_t* fixed);
