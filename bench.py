@@ -48,10 +48,10 @@ KERNELS = ("sweep_x", "sweep_y", "sweep_z")
 #   reverse step: transposed z reads lambda, u2, lo2, ip2, writes mu2 (5); transposed y reads M, mu2, u1, lo1,
 #   ip1, writes mu1 (6); transposed x the same for mu0 (6); update reads gx, gy, gz, T, y0, y1, y2, mu0, mu1,
 #   mu2, lambda and the five accumulators and writes lambda and the accumulators (22)          -> 39 arrays
-# so one gradient evaluation moves (23 + 23 + 39) * 8 = 680 B and does about 25 + 25 + 51 = 101 FP64
-# operations per voxel and step.
+# so one gradient evaluation moves (23 + 23 + 39) * 8 = 680 B and does about 25 + 25 + (3 + 4 + 4 + 34) = 95
+# FP64 operations per voxel and step (forward step, recompute, transposed solves and update).
 ADJ_BYTES_PER_VOXEL_STEP = (23 + 23 + 39) * 8
-ADJ_FP64_OPS_PER_VOXEL_STEP = 101
+ADJ_FP64_OPS_PER_VOXEL_STEP = 95
 
 
 def parse_args():

@@ -439,36 +439,39 @@ __global__ void adj_update_kernel(AView v, const double* __restrict__ gx, const 
   if (p >= v.nvox) return;
   const Vox x = vox_at(v, p);
   const double m0 = mu0[p], Tp = T[p];
-  double lt = 0.0;
-  if (x.i > 0) lt += gx[p] * (mu0[p - 1] - m0);
-  if (x.i + 1 < x.nx) lt += gx[p + 1] * (mu0[p + 1] - m0);
-  if (x.j > 0) lt += gy[p] * (mu0[p - x.nx] - m0);
-  if (x.j + 1 < x.ny) lt += gy[p + x.nx] * (mu0[p + x.nx] - m0);
-  if (x.k > 0) lt += gz[p] * (mu0[p - x.nxy] - m0);
-  if (x.k + 1 < x.nz) lt += gz[p + x.nxy] * (mu0[p + x.nxy] - m0);
-  double l = lam[p] + lt;
+  const double m1 = mu1[p], m2 = mu2[p];
+  const double a0 = y0[p], a1 = y1[p], a2 = y2[p];
+  // each low-face difference of mu0 serves both lambda's update (L mu0) and that face's gradient
+  double l = lam[p];
+  if (x.i > 0) {
+    const int64_t q = p - 1;
+    const double d0 = m0 - mu0[q];
+    l = fma(-gx[p], d0, l);
+    ggx[p] = fma(-d0, fma(0.5, a0 - y0[q], Tp - T[q]), ggx[p]);
+  }
+  if (x.j > 0) {
+    const int64_t q = p - x.nx;
+    const double d0 = m0 - mu0[q];
+    l = fma(-gy[p], d0, l);
+    ggy[p] = fma(-0.5 * (m1 - mu1[q]), a1 - y1[q], fma(-d0, Tp - T[q], ggy[p]));
+  }
+  if (x.k > 0) {
+    const int64_t q = p - x.nxy;
+    const double d0 = m0 - mu0[q];
+    l = fma(-gz[p], d0, l);
+    ggz[p] = fma(-0.5 * (m2 - mu2[q]), a2 - y2[q], fma(-d0, Tp - T[q], ggz[p]));
+  }
+  if (x.i + 1 < x.nx) l = fma(gx[p + 1], mu0[p + 1] - m0, l);
+  if (x.j + 1 < x.ny) l = fma(gy[p + x.nx], mu0[p + x.nx] - m0, l);
+  if (x.k + 1 < x.nz) l = fma(gz[p + x.nxy], mu0[p + x.nxy] - m0, l);
   if (obs_step >= 0 && x.k == 0) {
     const AInst& in = v.inst[x.inst];
     l += 2.0 * (Tp - obs[in.obs_off + obs_step * x.nxy + (p - in.off)]);
   }
   lam[p] = l;
-  const double m1 = mu1[p], m2 = mu2[p];
-  const double a0 = y0[p], a1 = y1[p], a2 = y2[p];
-  if (x.i > 0) {
-    const int64_t q = p - 1;
-    const double d0 = m0 - mu0[q];
-    ggx[p] += -d0 * (Tp - T[q]) - 0.5 * d0 * (a0 - y0[q]);
-  }
-  if (x.j > 0) {
-    const int64_t q = p - x.nx;
-    ggy[p] += -(m0 - mu0[q]) * (Tp - T[q]) - 0.5 * (m1 - mu1[q]) * (a1 - y1[q]);
-  }
-  if (x.k > 0) {
-    const int64_t q = p - x.nxy;
-    ggz[p] += -(m0 - mu0[q]) * (Tp - T[q]) - 0.5 * (m2 - mu2[q]) * (a2 - y2[q]);
-  }
-  gM[p] += m2 * a1 + m1 * a0 - m0 * a0 - m1 * a1 - m2 * a2;
-  gq[p] += s * m0;
+  // mu2 y1 + mu1 y0 - mu0 y0 - mu1 y1 - mu2 y2 = mu2 (y1 - y2) + mu1 (y0 - y1) - mu0 y0
+  gM[p] = fma(m2, a1 - a2, fma(m1, a0 - a1, fma(-m0, a0, gM[p])));
+  gq[p] = fma(s, m0, gq[p]);
 }
 
 // s + v as an unevaluated pair: returns the rounded sum, err receives its exact rounding error (Knuth's TwoSum)
