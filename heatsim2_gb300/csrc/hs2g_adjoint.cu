@@ -113,6 +113,19 @@ __global__ void adj_setup_kernel(AView v, const double* __restrict__ k, const do
   M[p] = C[p] * inv_dt;
 }
 
+// D = the sum of a voxel's six face conductances (the diagonal of -L)
+__global__ void adj_diag_kernel(AView v, const double* __restrict__ gx, const double* __restrict__ gy,
+                                const double* __restrict__ gz, double* __restrict__ D) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= v.nvox) return;
+  const Vox x = vox_at(v, p);
+  double d = gx[p] + gy[p] + gz[p];
+  if (x.i + 1 < x.nx) d += gx[p + 1];
+  if (x.j + 1 < x.ny) d += gy[p + x.nx];
+  if (x.k + 1 < x.nz) d += gz[p + x.nxy];
+  D[p] = d;
+}
+
 // factors of A_a = M - L_a/2 per line: lo (sub-diagonal), u (normalised super-diagonal), ip (1/pivot)
 __global__ void adj_factor_kernel(AView v, int axis, int64_t nlines, const double* __restrict__ M,
                                   const double* __restrict__ g, double* __restrict__ lo, double* __restrict__ u,
@@ -158,8 +171,9 @@ __device__ __forceinline__ XGroup xgroup(const AView& v, int64_t b) {
 // z_r = (r0_r - lo_r z_{r-1}) / piv_r, then back substitution y_r = z_r - u_r y_{r+1}
 __global__ void __launch_bounds__(kXT) adj_xfwd_kernel(AView v, const double* __restrict__ T,
                                                        const double* __restrict__ gx, const double* __restrict__ gy,
-                                                       const double* __restrict__ gz, const double* __restrict__ q,
-                                                       double s, const double* __restrict__ lo,
+                                                       const double* __restrict__ gz, const double* __restrict__ D,
+                                                       const double* __restrict__ q, double s,
+                                                       const double* __restrict__ lo,
                                                        const double* __restrict__ u, const double* __restrict__ ip,
                                                        double* __restrict__ y0) {
   __shared__ double sr[kXL][kXC + 1], sl[kXL][kXC + 1], si[kXL][kXC + 1];
@@ -177,14 +191,16 @@ __global__ void __launch_bounds__(kXT) adj_xfwd_kernel(AView v, const double* __
       if (l < g.nl && i < g.nx) {
         const int64_t line = g.l0 + l, j = line % g.ny, k = line / g.ny;
         const int64_t p = g.off + line * g.nx + i;
-        const double Tp = T[p];
-        double r = s * q[p];
-        if (i > 0) r += gx[p] * (T[p - 1] - Tp);
-        if (i + 1 < g.nx) r += gx[p + 1] * (T[p + 1] - Tp);
-        if (j > 0) r += gy[p] * (T[p - g.nx] - Tp);
-        if (j + 1 < g.ny) r += gy[p + g.nx] * (T[p + g.nx] - Tp);
-        if (k > 0) r += gz[p] * (T[p - nxy] - Tp);
-        if (k + 1 < g.nz) r += gz[p + nxy] * (T[p + nxy] - Tp);
+        // r0 = s q - D T_p + sum over faces of G T_nbr (D = the sum of the six G): 8 FP64 operations against 13
+        // for the face-by-face differences; temperatures are offsets from their initial mean, so the
+        // cancellation in -D T_p + sum G T_nbr stays at the rounding of the increments
+        double r = fma(-D[p], T[p], s * q[p]);
+        if (i > 0) r = fma(gx[p], T[p - 1], r);
+        if (i + 1 < g.nx) r = fma(gx[p + 1], T[p + 1], r);
+        if (j > 0) r = fma(gy[p], T[p - g.nx], r);
+        if (j + 1 < g.ny) r = fma(gy[p + g.nx], T[p + g.nx], r);
+        if (k > 0) r = fma(gz[p], T[p - nxy], r);
+        if (k + 1 < g.nz) r = fma(gz[p + nxy], T[p + nxy], r);
         sr[l][lane] = r;
         sl[l][lane] = lo[p];
         si[l][lane] = ip[p];
@@ -560,7 +576,7 @@ struct hs2g_adjoint {
   int64_t* xg_off = nullptr;
   int64_t nxgroups = 0;
   // parameters and derived fields
-  double *k = nullptr, *C = nullptr, *q = nullptr, *M = nullptr;
+  double *k = nullptr, *C = nullptr, *q = nullptr, *M = nullptr, *D = nullptr;
   double* g[3] = {nullptr, nullptr, nullptr};
   double *lo[3] = {nullptr, nullptr, nullptr}, *u[3] = {nullptr, nullptr, nullptr},
          *ip[3] = {nullptr, nullptr, nullptr};
@@ -638,7 +654,7 @@ cudaError_t grow(double** p, int64_t* cap, int64_t need) {
 cudaError_t fwd_step(hs2g_adjoint* a, cudaStream_t st, const double* T_in, double* T_out, double* y0, double* y1,
                      double* y2, double s) {
   const hs2g::AView v = view(a);
-  hs2g::adj_xfwd_kernel<<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(v, T_in, a->g[0], a->g[1], a->g[2], a->q, s,
+  hs2g::adj_xfwd_kernel<<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(v, T_in, a->g[0], a->g[1], a->g[2], a->D, a->q, s,
                                                                       a->lo[0], a->u[0], a->ip[0], y0);
   hs2g::adj_ysolve_kernel<<<line_blocks(a->nlines[1]), line_threads(a->nlines[1]), 0, st>>>(
       v, 1, a->nlines[1], a->M, y0, a->lo[1], a->u[1], a->ip[1], y1, nullptr, nullptr);
@@ -665,8 +681,8 @@ cudaError_t bwd_step(hs2g_adjoint* a, const double* Tn, const double* y0, const 
 }
 
 void adj_free(hs2g_adjoint* a) {
-  void* ptrs[] = {a->inst, a->vox_off, a->line_off, a->xg_off, a->k, a->C, a->q, a->M, a->g[0], a->g[1], a->g[2],
-                  a->lo[0], a->lo[1], a->lo[2], a->u[0], a->u[1], a->u[2], a->ip[0], a->ip[1], a->ip[2],
+  void* ptrs[] = {a->inst, a->vox_off, a->line_off, a->xg_off, a->k, a->C, a->q, a->M, a->D, a->g[0], a->g[1],
+                  a->g[2], a->lo[0], a->lo[1], a->lo[2], a->u[0], a->u[1], a->u[2], a->ip[0], a->ip[1], a->ip[2],
                   a->obs, a->ckpts, a->seg, a->seg2, a->T, a->lam, a->mu[0], a->mu[1], a->mu[2], a->gg[0], a->gg[1],
                   a->gg[2], a->gM, a->gq, a->parts};
   for (void* p : ptrs)
@@ -751,7 +767,7 @@ int hs2g_adjoint_create(int n, const hs2g_adjoint_grid* grids, double dt, int de
   if (e == cudaSuccess) e = cudaMalloc(&a->vox_off, sizeof(int64_t) * (n + 1));
   if (e == cudaSuccess) e = cudaMalloc(&a->line_off, sizeof(int64_t) * 3 * (n + 1));
   if (e == cudaSuccess) e = cudaMalloc(&a->xg_off, sizeof(int64_t) * (n + 1));
-  double** per_voxel[] = {&a->k, &a->C, &a->q, &a->M, &a->g[0], &a->g[1], &a->g[2], &a->lo[0], &a->lo[1],
+  double** per_voxel[] = {&a->k, &a->C, &a->q, &a->M, &a->D, &a->g[0], &a->g[1], &a->g[2], &a->lo[0], &a->lo[1],
                           &a->lo[2], &a->u[0], &a->u[1], &a->u[2], &a->ip[0], &a->ip[1], &a->ip[2], &a->T,
                           &a->lam, &a->mu[0], &a->mu[1], &a->mu[2], &a->gg[0], &a->gg[1], &a->gg[2], &a->gM,
                           &a->gq};
@@ -819,6 +835,7 @@ int hs2g_adjoint_set_parameters(hs2g_adjoint* a, const double* k, const double* 
   if (e != cudaSuccess) return acuda(e, "hs2g_adjoint_set_parameters");
   const hs2g::AView v = view(a);
   hs2g::adj_setup_kernel<<<nblk(n), kTh, 0, st>>>(v, a->k, a->C, 1.0 / a->dt, a->g[0], a->g[1], a->g[2], a->M);
+  hs2g::adj_diag_kernel<<<nblk(n), kTh, 0, st>>>(v, a->g[0], a->g[1], a->g[2], a->D);
   for (int ax = 0; ax < 3; ++ax)
     hs2g::adj_factor_kernel<<<nblk(a->nlines[ax]), kTh, 0, st>>>(v, ax, a->nlines[ax], a->M, a->g[ax], a->lo[ax],
                                                                 a->u[ax], a->ip[ax]);

@@ -91,17 +91,38 @@ def lap(T, gz, gy, gx):
     return out
 
 
+def residual(T, q, s, gz, gy, gx, D):
+    """s q - D T + sum over faces of G T_nbr, the forward x stage's residual (adj_xfwd_kernel)."""
+    r = s * q - D * T
+    r[:, :, 1:] += gx[:, :, 1:] * T[:, :, :-1]
+    r[:, :, :-1] += gx[:, :, 1:] * T[:, :, 1:]
+    r[:, 1:] += gy[:, 1:] * T[:, :-1]
+    r[:, :-1] += gy[:, 1:] * T[:, 1:]
+    r[1:] += gz[1:] * T[:-1]
+    r[:-1] += gz[1:] * T[1:]
+    return r
+
+
+def diagonal(gz, gy, gx):
+    D = gz + gy + gx
+    D[:, :, :-1] += gx[:, :, 1:]
+    D[:, :-1] += gy[:, 1:]
+    D[:-1] += gz[1:]
+    return D
+
+
 class Model(object):
     def __init__(self, k, C, q, dt, spacing):
         self.k, self.C, self.q, self.dt, self.spacing = k, C, q, dt, spacing
         self.g = low_faces(k, spacing)
+        self.D = diagonal(*self.g)
         self.M = C * (1.0 / dt)
         gz, gy, gx = self.g
         self.f = [factor(self.M, gx, 2), factor(self.M, gy, 1), factor(self.M, gz, 0)]
 
     def fwd_step(self, T, s):
         gz, gy, gx = self.g
-        y0 = solve(self.f[0], lap(T, gz, gy, gx) + s * self.q, 2)
+        y0 = solve(self.f[0], residual(T, self.q, s, gz, gy, gx, self.D), 2)
         y1 = solve(self.f[1], self.M * y0, 1)
         y2 = solve(self.f[2], self.M * y1, 0)
         return T + y2, y0, y1, y2
