@@ -469,9 +469,10 @@ cudaError_t batch_autotune(Batch& b, std::string& report) {
   // x: persistent grid size (CTAs of 128 threads)
   {
     float bt = 1e30f;
-    for (int per : {4, 5, 6, 7, 8, 10}) {
+    // per = 0: one CTA per work item, the hardware's block scheduler doing the balancing
+    for (int per : {4, 5, 6, 7, 8, 10, 0}) {
       Tuning t = best;
-      t.x_grid = (int)std::min<int64_t>(b.nxw, (int64_t)sms * per);
+      t.x_grid = (int)std::min<int64_t>(std::min<int64_t>(b.nxw, 1 << 30), per ? (int64_t)sms * per : b.nxw);
       float ms;
       if ((e = batch_time_axis(b, 0, t, 2, &ms)) != cudaSuccess) return e;
       snprintf(line, sizeof line, "x grid %d: %.3f ms\n", t.x_grid, ms);
@@ -752,7 +753,7 @@ int hs2g_batch_create(int n, const hs2g_class_problem* problems, int precision, 
   if ((e = hs2g::batch_upload_work(b, 128, 128)) != cudaSuccess) return bail(bcuda(e, "work lists"));
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  b.tune.x_grid = (int)std::min<int64_t>(b.nxw, (int64_t)sms * 8);
+  b.tune.x_grid = (int)std::min<int64_t>(b.nxw, (int64_t)sms * 7);  // the x kernel's 7 resident CTAs per SM
   b.tune.y_grid = (int)std::min<int64_t>(b.nyw, (int64_t)sms * 16);
   b.tune.z_grid = (int)std::min<int64_t>(b.nzw, (int64_t)sms * 16);
   if ((e = cudaStreamSynchronize(b.stream)) != cudaSuccess) return bail(bcuda(e, "batch create"));
