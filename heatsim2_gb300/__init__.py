@@ -10,7 +10,12 @@ Drop-in for the reference package's hot path (isuthermography/heatsim2, heatsim2
 
 Same material / boundary / source tuples, the same four boundary-class modules and the same uint8 class
 arrays.  ``install_as_heatsim2()`` registers this package under the name ``heatsim2`` so existing scripts and
-user boundary classes that import ``heatsim2.expression.group`` run unchanged.
+user boundary classes that import ``heatsim2.expression.group`` run unchanged.  ``setup`` also takes the
+reference's surface-curvature arrays (curved-surface mode, ``heatsim2_gb300.curvature``).
+
+Beside the drop-in: ``heatsim2_gb300.batch.Batch`` advances many problems of uneven size together (FP64, or
+FP32 with its error against FP64 measured), and ``heatsim2_gb300.adjoint`` gives gradients of a surface
+misfit with respect to per-voxel conductivity, heat capacity and source (``torch.autograd.Function`` forms).
 """
 import os
 import sys

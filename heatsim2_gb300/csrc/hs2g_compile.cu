@@ -1,5 +1,6 @@
 // Setup-time kernels: the coefficient compiler (class arrays -> per-face conductances) and the per-line
-// tridiagonal factorisations that turn conductances and capacities into the step coefficients.
+// tridiagonal factorisations that turn conductances (shared per face, or per row in the curved-surface mode)
+// and capacities into the step coefficients.
 //
 // Replaces the reference's Python voxel loop and symbolic assembly (crank_nicolson.pyx:272-491,
 // alternatingdirection_c.c:102-199) and its LU factorisation at finalize (tridiag.pyx:9-43,
