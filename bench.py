@@ -12,7 +12,9 @@ throw-away copy.  Synthetic, seeded input (heatsim2_gb300.workloads.composite_pa
 Prints one JSON line.  ``value`` counts computed voxels (64*512*512) per second with the state resident in
 HBM; ``e2e`` is the same metric through the C ABI with host buffers (host->device copy of T, the step,
 device->host copy of T, every step); ``roofline`` is the dominant sweep kernel against the measured HBM copy
-bandwidth; ``fp64_roofline`` the whole step against the measured FP64 FMA rate, the resource that binds;
+bandwidth; ``step_hbm`` the whole step against it (this implementation's bytes, and the 136-byte accounting
+of a step that re-reads T, M and the face conductances in every sweep); ``fp64_roofline`` the whole step
+against the measured FP64 FMA rate, the resource that binds;
 ``cpu_baseline`` the reference (or, where it cannot be built, the oracle) on the host cores.  ``batched`` is
 the 256-instance uneven batch (FP64 and FP32) against a per-instance loop of the plain path; ``adjoint`` the
 gradient evaluations per second of the (32,128,128) steel inverse problem and of the 32-instance batched
@@ -559,6 +561,13 @@ def gpu_arm(args, world, rank, local_rank):
     fp64["frac"] = fp64["achieved"] / fp64["peak"] if fp64["peak"] else None
     per_kernel_fp64 = {k: FP64_OPS_PER_VOXEL[k] * grid_vox / (per_kernel_ms[k] * 1e-3) / fma_rate.value
                        for k in KERNELS}
+    # the whole step against HBM: with this implementation's algorithmic bytes (160 per grid voxel), and with
+    # the 136-byte accounting of a step that re-reads T, M and the face conductances in every sweep (17 arrays)
+    step_s = total_ms * 1e-3 / K
+    step_hbm = {"bytes_per_voxel_step": sum(BYTES_PER_VOXEL.values()),
+                "achieved_gbs": sum(BYTES_PER_VOXEL.values()) * grid_vox / step_s / 1e9,
+                "frac": sum(BYTES_PER_VOXEL.values()) * grid_vox / step_s / 1e9 / hbm_peak,
+                "frac_136_bytes": 136 * compute_vox / step_s / 1e9 / hbm_peak, "peak": hbm_peak}
     per_kernel_hbm = {k: BYTES_PER_VOXEL[k] * grid_vox / (per_kernel_ms[k] * 1e-3) / 1e9 / hbm_peak
                       for k in KERNELS}
     # end to end through the C ABI with pinned host buffers
@@ -611,7 +620,7 @@ def gpu_arm(args, world, rank, local_rank):
                              % (grid_vox * 8 / 1e6, state_bytes / 1e6),
                        "kernels": "x: CTA-staged stencil + warp recurrence; y: TMA tensor-tile ring; z: per-line",
                        "parallelism": "replicas" if world > 1 else "single"},
-            "roofline": roofline, "fp64_roofline": fp64,
+            "roofline": roofline, "fp64_roofline": fp64, "step_hbm": step_hbm,
             "kernel_ms_per_step": per_kernel_ms, "kernel_fp64_frac": per_kernel_fp64,
             "kernel_hbm_frac": per_kernel_hbm,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * K, "clocks": clk, "setup_s": setup_s,
