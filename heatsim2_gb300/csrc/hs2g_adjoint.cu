@@ -167,6 +167,25 @@ __device__ __forceinline__ XGroup xgroup(const AView& v, int64_t b) {
   return g;
 }
 
+// r0 = s q - D T_p + sum over faces of G T_nbr at voxel p = (k, j, i) of an (nz, ny, nx) instance (D = the sum
+// of the six G): 8 FP64 operations against 13 for the face-by-face differences; temperatures are offsets
+// from their initial mean, so the cancellation in -D T_p + sum G T_nbr stays at the rounding of the increments
+__device__ __forceinline__ double residual_at(const double* __restrict__ T, const double* __restrict__ gx,
+                                              const double* __restrict__ gy, const double* __restrict__ gz,
+                                              const double* __restrict__ D, const double* __restrict__ q, double s,
+                                              int64_t p, int64_t i, int64_t j, int64_t k, int64_t nx, int64_t ny,
+                                              int64_t nz) {
+  const int64_t nxy = nx * ny;
+  double r = __fma_rn(-D[p], T[p], __dmul_rn(s, q[p]));
+  if (i > 0) r = __fma_rn(gx[p], T[p - 1], r);
+  if (i + 1 < nx) r = __fma_rn(gx[p + 1], T[p + 1], r);
+  if (j > 0) r = __fma_rn(gy[p], T[p - nx], r);
+  if (j + 1 < ny) r = __fma_rn(gy[p + nx], T[p + nx], r);
+  if (k > 0) r = __fma_rn(gz[p], T[p - nxy], r);
+  if (k + 1 < nz) r = __fma_rn(gz[p + nxy], T[p + nxy], r);
+  return r;
+}
+
 // forward x stage fused with the residual r0 = L T + s q: y0 = A_x^-1 r0, forward elimination
 // z_r = (r0_r - lo_r z_{r-1}) / piv_r, then back substitution y_r = z_r - u_r y_{r+1}
 __global__ void __launch_bounds__(kXT) adj_xfwd_kernel(AView v, const double* __restrict__ T,
@@ -180,7 +199,6 @@ __global__ void __launch_bounds__(kXT) adj_xfwd_kernel(AView v, const double* __
   const XGroup g = xgroup(v, blockIdx.x);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr int kPer = kXL / (kXT / 32);
-  const int64_t nxy = g.nx * g.ny;
   const int nch = (int)((g.nx + kXC - 1) / kXC);
   double carry = 0.0;
   for (int ch = 0; ch < nch; ++ch) {
@@ -191,17 +209,7 @@ __global__ void __launch_bounds__(kXT) adj_xfwd_kernel(AView v, const double* __
       if (l < g.nl && i < g.nx) {
         const int64_t line = g.l0 + l, j = line % g.ny, k = line / g.ny;
         const int64_t p = g.off + line * g.nx + i;
-        // r0 = s q - D T_p + sum over faces of G T_nbr (D = the sum of the six G): 8 FP64 operations against 13
-        // for the face-by-face differences; temperatures are offsets from their initial mean, so the
-        // cancellation in -D T_p + sum G T_nbr stays at the rounding of the increments
-        double r = fma(-D[p], T[p], s * q[p]);
-        if (i > 0) r = fma(gx[p], T[p - 1], r);
-        if (i + 1 < g.nx) r = fma(gx[p + 1], T[p + 1], r);
-        if (j > 0) r = fma(gy[p], T[p - g.nx], r);
-        if (j + 1 < g.ny) r = fma(gy[p + g.nx], T[p + g.nx], r);
-        if (k > 0) r = fma(gz[p], T[p - nxy], r);
-        if (k + 1 < g.nz) r = fma(gz[p + nxy], T[p + nxy], r);
-        sr[l][lane] = r;
+        sr[l][lane] = residual_at(T, gx, gy, gz, D, q, s, p, i, j, k, g.nx, g.ny, g.nz);
         sl[l][lane] = lo[p];
         si[l][lane] = ip[p];
       }
@@ -211,7 +219,7 @@ __global__ void __launch_bounds__(kXT) adj_xfwd_kernel(AView v, const double* __
       const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
       double z = carry;
       for (int cc = 0; cc < cw; ++cc) {
-        z = (sr[lane][cc] - sl[lane][cc] * z) * si[lane][cc];
+        z = __dmul_rn(__fma_rn(-sl[lane][cc], z, sr[lane][cc]), si[lane][cc]);
         sr[lane][cc] = z;
       }
       carry = z;
@@ -239,7 +247,7 @@ __global__ void __launch_bounds__(kXT) adj_xfwd_kernel(AView v, const double* __
       const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
       double x = carry;
       for (int cc = cw - 1; cc >= 0; --cc) {
-        x = sr[lane][cc] - sl[lane][cc] * x;
+        x = __fma_rn(-sl[lane][cc], x, sr[lane][cc]);
         sr[lane][cc] = x;
       }
       carry = x;
@@ -271,7 +279,7 @@ __global__ void __launch_bounds__(kXT) adj_xsolve_t_kernel(AView v, const double
       const int l = warp * kPer + ll;
       if (l < g.nl && i < g.nx) {
         const int64_t p = g.off + (g.l0 + l) * g.nx + i;
-        sb[l][lane] = M[p] * rhs[p];
+        sb[l][lane] = __dmul_rn(M[p], rhs[p]);
         sl[l][lane] = u[p];
       }
     }
@@ -279,7 +287,7 @@ __global__ void __launch_bounds__(kXT) adj_xsolve_t_kernel(AView v, const double
     if (warp == 0 && lane < g.nl) {
       const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
       for (int cc = 0; cc < cw; ++cc) {
-        w = sb[lane][cc] - u_prev * w;
+        w = __fma_rn(-u_prev, w, sb[lane][cc]);
         u_prev = sl[lane][cc];
         sb[lane][cc] = w;
       }
@@ -307,7 +315,7 @@ __global__ void __launch_bounds__(kXT) adj_xsolve_t_kernel(AView v, const double
     if (warp == 0 && lane < g.nl) {
       const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
       for (int cc = cw - 1; cc >= 0; --cc) {
-        x = (sb[lane][cc] - lo_next * x) * si[lane][cc];
+        x = __dmul_rn(__fma_rn(-lo_next, x, sb[lane][cc]), si[lane][cc]);
         lo_next = sl[lane][cc];
         sb[lane][cc] = x;
       }
@@ -324,7 +332,9 @@ __global__ void __launch_bounds__(kXT) adj_xsolve_t_kernel(AView v, const double
 // y / z stage, forward: y = A_a^-1 (M rhs) along each strided line (one thread per line, neighbouring
 // threads on neighbouring lines, so every row access is coalesced); T_out = T_in + y when T_out is given.
 // Rows go in blocks of kRB: the loads of a block are issued together, then the recurrence runs through it,
-// so a line pays one memory latency per block instead of one per row.
+// so a line pays one memory latency per block instead of one per row.  The rounding of every operation is
+// explicit (no contraction left to the compiler) so that the few-line kernels below, which stage rows
+// differently, give the same bits.
 constexpr int kRB = 8;
 
 __global__ void __launch_bounds__(128, 4) adj_ysolve_kernel(AView v, int axis, int64_t nlines, const double* __restrict__ M,
@@ -342,7 +352,7 @@ __global__ void __launch_bounds__(128, 4) adj_ysolve_kernel(AView v, int axis, i
     for (int e = 0; e < kRB; ++e) {
       if (r0 + e < ln.len) {
         const int64_t p = ln.base + (r0 + e) * ln.stride;
-        b[e] = M[p] * rhs[p];
+        b[e] = __dmul_rn(M[p], rhs[p]);
         l[e] = lo[p];
         iv[e] = ip[p];
       }
@@ -350,7 +360,7 @@ __global__ void __launch_bounds__(128, 4) adj_ysolve_kernel(AView v, int axis, i
 #pragma unroll
     for (int e = 0; e < kRB; ++e) {
       if (r0 + e < ln.len) {
-        z = (b[e] - l[e] * z) * iv[e];
+        z = __dmul_rn(__fma_rn(-l[e], z, b[e]), iv[e]);
         y[ln.base + (r0 + e) * ln.stride] = z;
       }
     }
@@ -371,9 +381,9 @@ __global__ void __launch_bounds__(128, 4) adj_ysolve_kernel(AView v, int axis, i
     for (int e = 0; e < kRB; ++e) {
       if (r1 - e >= 0) {
         const int64_t p = ln.base + (r1 - e) * ln.stride;
-        x = yy[e] - uu[e] * x;
+        x = __fma_rn(-uu[e], x, yy[e]);
         y[p] = x;
-        if (T_out) T_out[p] = tt[e] + x;
+        if (T_out) T_out[p] = __dadd_rn(tt[e], x);
       }
     }
   }
@@ -395,14 +405,14 @@ __global__ void __launch_bounds__(128, 4) adj_ysolve_t_kernel(AView v, int axis,
     for (int e = 0; e < kRB; ++e) {
       if (r0 + e < ln.len) {
         const int64_t p = ln.base + (r0 + e) * ln.stride;
-        b[e] = M ? M[p] * rhs[p] : rhs[p];
+        b[e] = M ? __dmul_rn(M[p], rhs[p]) : rhs[p];
         uu[e] = u[p];
       }
     }
 #pragma unroll
     for (int e = 0; e < kRB; ++e) {
       if (r0 + e < ln.len) {
-        w = b[e] - u_prev * w;
+        w = __fma_rn(-u_prev, w, b[e]);
         u_prev = uu[e];
         mu[ln.base + (r0 + e) * ln.stride] = w;
       }
@@ -423,12 +433,363 @@ __global__ void __launch_bounds__(128, 4) adj_ysolve_t_kernel(AView v, int axis,
 #pragma unroll
     for (int e = 0; e < kRB; ++e) {
       if (r1 - e >= 0) {
-        x = (ww[e] - lo_next * x) * iv[e];
+        x = __dmul_rn(__fma_rn(-lo_next, x, ww[e]), iv[e]);
         lo_next = l[e];
         mu[ln.base + (r1 - e) * ln.stride] = x;
       }
     }
   }
+}
+
+// Few-line forms of the two kernels above.  A small problem (4096 y-lines of 128 rows at 32x128x128) leaves
+// each SM about one warp, whose line is then a chain of memory round trips, one per block of rows.  Here a
+// 32-thread CTA streams its lines' rows through a ring of kFS stages of kFR rows with cp.async (each thread
+// copies its own line's elements, so no barrier is needed), keeping up to (kFS - 1) * kFR rows in flight, and
+// holds the first pass's values of the whole line in shared memory for the second pass.  Same operations,
+// same order, same rounding as adj_ysolve_kernel / adj_ysolve_t_kernel.
+// What remains is the FP64 chain: GB300 issues a warp's FP64 instruction over ~60 cycles of its
+// sub-partition's pipe whatever the number of active lanes (0.54 lanes per clock), so a 128-row line of the
+// five-operation forward solve takes ~20 us however the lines are spread over warps (measured: four 8-lane
+// warps per 32 lines gave the same y time and doubled the z time).
+constexpr int kFS = 4;            // ring stages
+constexpr int kFR = 8;            // rows per stage
+constexpr int kFewMaxLen = 512;   // longest line the few-line kernels hold (128 KB of line values)
+
+__device__ __forceinline__ void cp_async8(double* dst, const double* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_ring() { cp_async_wait<kFS - 1>(); }
+
+// dynamic shared memory of a few-line launch: the line values, then the ring of up to 4 operands
+inline size_t few_smem_bytes(int64_t max_len) {
+  return sizeof(double) * 32 * (size_t)(max_len + kFS * kFR * 4);
+}
+
+// Streams `nops` operands of rows r(g, e) of block g into ring slot g % kFS; rows outside the line are skipped.
+// Always commits a group, so that exactly kFS - 1 groups are younger than the one the consumer waits for.
+struct FewRing {
+  double* ring;
+  int lane;
+  __device__ __forceinline__ double* at(int g, int e, int a) const {
+    return ring + (((g % kFS) * kFR + e) * 4 + a) * 32 + lane;
+  }
+};
+
+__global__ void __launch_bounds__(32) adj_ysolve_few_kernel(AView v, int axis, int64_t nlines, int64_t max_len,
+                                                            const double* __restrict__ M,
+                                                            const double* __restrict__ rhs,
+                                                            const double* __restrict__ lo,
+                                                            const double* __restrict__ u,
+                                                            const double* __restrict__ ip, double* y,
+                                                            const double* T_in, double* T_out) {
+  extern __shared__ double few_sm[];
+  const int lane = threadIdx.x;
+  const int64_t t = blockIdx.x * (int64_t)32 + lane;
+  if (t >= nlines) return;
+  const Line ln = line_at(v, axis, t);
+  double* line = few_sm;  // line[r * 32 + lane]
+  const FewRing R{few_sm + 32 * max_len, lane};
+  const int len = (int)ln.len, nb = (len + kFR - 1) / kFR;
+  auto issue_fwd = [&](int g) {
+    if (g < nb)
+      for (int e = 0; e < kFR; ++e) {
+        const int r = g * kFR + e;
+        if (r < len) {
+          const int64_t p = ln.base + r * ln.stride;
+          cp_async8(R.at(g, e, 0), M + p);
+          cp_async8(R.at(g, e, 1), rhs + p);
+          cp_async8(R.at(g, e, 2), lo + p);
+          cp_async8(R.at(g, e, 3), ip + p);
+        }
+      }
+    cp_async_commit();
+  };
+  for (int g = 0; g < kFS - 1; ++g) issue_fwd(g);
+  double z = 0.0;
+  for (int g = 0; g < nb; ++g) {
+    issue_fwd(g + kFS - 1);  // into the slot consumed in the previous iteration
+    cp_async_wait_ring();
+    for (int e = 0; e < kFR; ++e) {
+      const int r = g * kFR + e;
+      if (r < len) {
+        const double b = __dmul_rn(*R.at(g, e, 0), *R.at(g, e, 1));
+        z = __dmul_rn(__fma_rn(-*R.at(g, e, 2), z, b), *R.at(g, e, 3));
+        line[r * 32 + lane] = z;
+      }
+    }
+  }
+  auto issue_bwd = [&](int g) {
+    if (g < nb)
+      for (int e = 0; e < kFR; ++e) {
+        const int r = len - 1 - (g * kFR + e);
+        if (r >= 0) {
+          const int64_t p = ln.base + r * ln.stride;
+          cp_async8(R.at(g, e, 0), u + p);
+          if (T_out) cp_async8(R.at(g, e, 1), T_in + p);
+        }
+      }
+    cp_async_commit();
+  };
+  for (int g = 0; g < kFS - 1; ++g) issue_bwd(g);
+  double x = 0.0;
+  for (int g = 0; g < nb; ++g) {
+    issue_bwd(g + kFS - 1);
+    cp_async_wait_ring();
+    for (int e = 0; e < kFR; ++e) {
+      const int r = len - 1 - (g * kFR + e);
+      if (r >= 0) {
+        const int64_t p = ln.base + r * ln.stride;
+        x = __fma_rn(-*R.at(g, e, 0), x, line[r * 32 + lane]);
+        y[p] = x;
+        if (T_out) T_out[p] = __dadd_rn(*R.at(g, e, 1), x);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(32) adj_ysolve_t_few_kernel(AView v, int axis, int64_t nlines, int64_t max_len,
+                                                              const double* __restrict__ M,
+                                                              const double* __restrict__ rhs,
+                                                              const double* __restrict__ lo,
+                                                              const double* __restrict__ u,
+                                                              const double* __restrict__ ip,
+                                                              double* __restrict__ mu) {
+  extern __shared__ double few_sm[];
+  const int lane = threadIdx.x;
+  const int64_t t = blockIdx.x * (int64_t)32 + lane;
+  if (t >= nlines) return;
+  const Line ln = line_at(v, axis, t);
+  double* line = few_sm;
+  const FewRing R{few_sm + 32 * max_len, lane};
+  const int len = (int)ln.len, nb = (len + kFR - 1) / kFR;
+  auto issue_asc = [&](int g) {  // U^T w = b, rows ascending
+    if (g < nb)
+      for (int e = 0; e < kFR; ++e) {
+        const int r = g * kFR + e;
+        if (r < len) {
+          const int64_t p = ln.base + r * ln.stride;
+          cp_async8(R.at(g, e, 0), rhs + p);
+          cp_async8(R.at(g, e, 1), u + p);
+          if (M) cp_async8(R.at(g, e, 2), M + p);
+        }
+      }
+    cp_async_commit();
+  };
+  for (int g = 0; g < kFS - 1; ++g) issue_asc(g);
+  double w = 0.0, u_prev = 0.0;
+  for (int g = 0; g < nb; ++g) {
+    issue_asc(g + kFS - 1);
+    cp_async_wait_ring();
+    for (int e = 0; e < kFR; ++e) {
+      const int r = g * kFR + e;
+      if (r < len) {
+        const double b = M ? __dmul_rn(*R.at(g, e, 2), *R.at(g, e, 0)) : *R.at(g, e, 0);
+        w = __fma_rn(-u_prev, w, b);
+        u_prev = *R.at(g, e, 1);
+        line[r * 32 + lane] = w;
+      }
+    }
+  }
+  auto issue_desc = [&](int g) {  // Lo^T x = w, rows descending
+    if (g < nb)
+      for (int e = 0; e < kFR; ++e) {
+        const int r = len - 1 - (g * kFR + e);
+        if (r >= 0) {
+          const int64_t p = ln.base + r * ln.stride;
+          cp_async8(R.at(g, e, 0), lo + p);
+          cp_async8(R.at(g, e, 1), ip + p);
+        }
+      }
+    cp_async_commit();
+  };
+  for (int g = 0; g < kFS - 1; ++g) issue_desc(g);
+  double x = 0.0, lo_next = 0.0;
+  for (int g = 0; g < nb; ++g) {
+    issue_desc(g + kFS - 1);
+    cp_async_wait_ring();
+    for (int e = 0; e < kFR; ++e) {
+      const int r = len - 1 - (g * kFR + e);
+      if (r >= 0) {
+        x = __dmul_rn(__fma_rn(-lo_next, x, line[r * 32 + lane]), *R.at(g, e, 1));
+        lo_next = *R.at(g, e, 0);
+        mu[ln.base + r * ln.stride] = x;
+      }
+    }
+  }
+}
+
+// Few-line forms of the x stages.  A 32-line group of a small problem is a latency chain in
+// adj_xfwd_kernel (four dependent load rounds per 32-column chunk); here each of four warps streams the
+// chunks of kFewLanes of the group's lines through a ring of kXFS tiles with cp.async (lane = column,
+// row-contiguous copies), recurs with lane = line while the next two chunks are in flight, keeps the whole
+// lines in shared memory between the two passes and stores them once, row-contiguous.  The residual r0 comes from adj_resid_kernel (one thread per voxel)
+// instead of being fused.  Same operations, same order, same rounding as the fused kernels.
+constexpr int kXFS = 3;              // ring stages (tiles of kXL lines x kXC columns x 3 operands)
+constexpr int kFewLanes = 8;         // lines per warp (four warps per group: the copies spread over them)
+constexpr int kFewXGroups = 2 * 152; // at most this many 32-line groups (two CTAs per SM at 128 columns)
+
+inline size_t few_x_smem_bytes(int64_t max_nx) {
+  return sizeof(double) * ((size_t)kXL * (size_t)(max_nx + 1) + (size_t)kXFS * 3 * kXL * (kXC + 1));
+}
+
+__global__ void adj_resid_kernel(AView v, const double* __restrict__ T, const double* __restrict__ gx,
+                                 const double* __restrict__ gy, const double* __restrict__ gz,
+                                 const double* __restrict__ D, const double* __restrict__ q, double s,
+                                 double* __restrict__ r0) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= v.nvox) return;
+  const Vox x = vox_at(v, p);
+  r0[p] = residual_at(T, gx, gy, gz, D, q, s, p, x.i, x.j, x.k, x.nx, x.ny, x.nz);
+}
+
+// the group's tiles and line buffer in dynamic shared memory: lines[l * (max_nx + 1) + c], then the ring
+struct FewX {
+  double* lines;
+  double* ring;
+  int64_t zs;
+  __device__ __forceinline__ double* tile(int seq, int a, int l) const {
+    return ring + (((seq % kXFS) * 3 + a) * kXL + l) * (kXC + 1);
+  }
+};
+
+// copies columns [ch * kXC, ch * kXC + kXC) of the group's lines of up to three operands into ring slot
+// seq % kXFS (nothing when ch is outside the line); always commits a group
+__device__ __forceinline__ void few_x_issue(const FewX& F, const XGroup& g, int seq, int ch, int lane, int l_begin,
+                                            int l_end, const double* a0, const double* a1, const double* a2) {
+  const int64_t c = (int64_t)ch * kXC + lane;
+  if (ch >= 0 && c < g.nx) {
+    const int64_t row0 = g.off + g.l0 * g.nx + c;
+    for (int l = l_begin; l < l_end; ++l) {
+      const int64_t p = row0 + (int64_t)l * g.nx;
+      cp_async8(F.tile(seq, 0, l) + lane, a0 + p);
+      if (a1) cp_async8(F.tile(seq, 1, l) + lane, a1 + p);
+      if (a2) cp_async8(F.tile(seq, 2, l) + lane, a2 + p);
+    }
+  }
+  cp_async_commit();
+}
+
+// the group's lines from the line buffer to global memory, row-contiguous
+__device__ __forceinline__ void few_x_store(const FewX& F, const XGroup& g, int lane, int l_begin, int l_end,
+                                            double* out) {
+  __syncwarp();
+  for (int l = l_begin; l < l_end; ++l)
+    for (int64_t c = lane; c < g.nx; c += 32) out[g.off + (g.l0 + l) * g.nx + c] = F.lines[l * F.zs + c];
+}
+
+// y0 = A_x^-1 r0 (r0 may alias y0), the arithmetic of adj_xfwd_kernel
+__global__ void __launch_bounds__(128) adj_xsolve_few_kernel(AView v, int64_t max_nx, const double* r0,
+                                                            const double* __restrict__ lo,
+                                                            const double* __restrict__ u,
+                                                            const double* __restrict__ ip, double* y0) {
+  extern __shared__ double few_sm[];
+  const XGroup g = xgroup(v, blockIdx.x);
+  // warp w solves the group's lines [lb, le): it copies them with lane = column and recurs with lane = line
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lb = min(warp * kFewLanes, (int)g.nl), le = min(lb + kFewLanes, (int)g.nl), ln = lb + lane;
+  const FewX F{few_sm, few_sm + kXL * (max_nx + 1), max_nx + 1};
+  const int nch = (int)((g.nx + kXC - 1) / kXC);
+  for (int q = 0; q < kXFS - 1; ++q) few_x_issue(F, g, q, q < nch ? q : -1, lane, lb, le, r0, lo, ip);
+  double z = 0.0;
+  for (int ch = 0; ch < nch; ++ch) {
+    __syncwarp();  // every lane is done with the slot refilled here
+    const int nxt = ch + kXFS - 1;
+    few_x_issue(F, g, nxt, nxt < nch ? nxt : -1, lane, lb, le, r0, lo, ip);
+    cp_async_wait<kXFS - 1>();
+    __syncwarp();  // chunk ch's copies by every lane are visible
+    if (ln < le) {
+      const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
+      const double *tr = F.tile(ch, 0, ln), *tl = F.tile(ch, 1, ln), *ti = F.tile(ch, 2, ln);
+      double* zr = F.lines + ln * F.zs + ch * kXC;
+      for (int cc = 0; cc < cw; ++cc) {
+        z = __dmul_rn(__fma_rn(-tl[cc], z, tr[cc]), ti[cc]);
+        zr[cc] = z;
+      }
+    }
+  }
+  __syncwarp();
+  for (int q = 0; q < kXFS - 1; ++q) few_x_issue(F, g, q, nch - 1 - q, lane, lb, le, u, nullptr, nullptr);
+  double x = 0.0;
+  for (int q = 0; q < nch; ++q) {
+    __syncwarp();
+    few_x_issue(F, g, q + kXFS - 1, nch - kXFS - q, lane, lb, le, u, nullptr, nullptr);
+    cp_async_wait<kXFS - 1>();
+    __syncwarp();
+    const int ch = nch - 1 - q;
+    if (ln < le) {
+      const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
+      const double* tu = F.tile(q, 0, ln);
+      double* zr = F.lines + ln * F.zs + ch * kXC;
+      for (int cc = cw - 1; cc >= 0; --cc) {
+        x = __fma_rn(-tu[cc], x, zr[cc]);
+        zr[cc] = x;
+      }
+    }
+  }
+  few_x_store(F, g, lane, lb, le, y0);
+}
+
+// mu = A_x^-T (M rhs), the arithmetic of adj_xsolve_t_kernel
+__global__ void __launch_bounds__(128) adj_xsolve_t_few_kernel(AView v, int64_t max_nx,
+                                                              const double* __restrict__ M,
+                                                              const double* __restrict__ rhs,
+                                                              const double* __restrict__ lo,
+                                                              const double* __restrict__ u,
+                                                              const double* __restrict__ ip,
+                                                              double* __restrict__ mu) {
+  extern __shared__ double few_sm[];
+  const XGroup g = xgroup(v, blockIdx.x);
+  // warp w solves the group's lines [lb, le): it copies them with lane = column and recurs with lane = line
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lb = min(warp * kFewLanes, (int)g.nl), le = min(lb + kFewLanes, (int)g.nl), ln = lb + lane;
+  const FewX F{few_sm, few_sm + kXL * (max_nx + 1), max_nx + 1};
+  const int nch = (int)((g.nx + kXC - 1) / kXC);
+  for (int q = 0; q < kXFS - 1; ++q) few_x_issue(F, g, q, q < nch ? q : -1, lane, lb, le, rhs, M, u);
+  double w = 0.0, u_prev = 0.0;
+  for (int ch = 0; ch < nch; ++ch) {  // U^T w = M rhs, rows ascending
+    __syncwarp();
+    const int nxt = ch + kXFS - 1;
+    few_x_issue(F, g, nxt, nxt < nch ? nxt : -1, lane, lb, le, rhs, M, u);
+    cp_async_wait<kXFS - 1>();
+    __syncwarp();
+    if (ln < le) {
+      const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
+      const double *tb = F.tile(ch, 0, ln), *tm = F.tile(ch, 1, ln), *tu = F.tile(ch, 2, ln);
+      double* zr = F.lines + ln * F.zs + ch * kXC;
+      for (int cc = 0; cc < cw; ++cc) {
+        w = __fma_rn(-u_prev, w, __dmul_rn(tm[cc], tb[cc]));
+        u_prev = tu[cc];
+        zr[cc] = w;
+      }
+    }
+  }
+  __syncwarp();
+  for (int q = 0; q < kXFS - 1; ++q) few_x_issue(F, g, q, nch - 1 - q, lane, lb, le, lo, ip, nullptr);
+  double x = 0.0, lo_next = 0.0;
+  for (int q = 0; q < nch; ++q) {  // Lo^T x = w, rows descending
+    __syncwarp();
+    few_x_issue(F, g, q + kXFS - 1, nch - kXFS - q, lane, lb, le, lo, ip, nullptr);
+    cp_async_wait<kXFS - 1>();
+    __syncwarp();
+    const int ch = nch - 1 - q;
+    if (ln < le) {
+      const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
+      const double *tl = F.tile(q, 0, ln), *ti = F.tile(q, 1, ln);
+      double* zr = F.lines + ln * F.zs + ch * kXC;
+      for (int cc = cw - 1; cc >= 0; --cc) {
+        x = __dmul_rn(__fma_rn(-lo_next, x, zr[cc]), ti[cc]);
+        lo_next = tl[cc];
+        zr[cc] = x;
+      }
+    }
+  }
+  few_x_store(F, g, lane, lb, le, mu);
 }
 
 // lambda = misfit gradient of the last observation, 2 (T_N - d_{N-1}) on the top layer, 0 below
@@ -503,7 +864,7 @@ __device__ __forceinline__ double two_sum(double s, double v, double& err) {
 // part[2*((step*ninst + i)*kMisfitBlocks + c)] and the next entry (rounded sum, error); summing the pairs
 // exactly on the host leaves the loss with no summation error that would swamp the small loss differences
 // finite-difference checks take
-constexpr int kMisfitBlocks = 8;
+constexpr int kMisfitBlocks = 32;
 __global__ void adj_misfit_kernel(AView v, const double* __restrict__ T, const double* __restrict__ obs,
                                   int64_t step, double* __restrict__ part) {
   __shared__ double sh_hi[256], sh_lo[256];
@@ -568,6 +929,7 @@ struct hs2g_adjoint {
   int ninst = 0;
   int64_t n = 0, nobs_step = 0;  // voxels; top-layer voxels of all instances (observations per step)
   int64_t nlines[3] = {0, 0, 0};
+  int64_t max_len[3] = {0, 0, 0};  // longest line of each axis over the instances
   std::vector<hs2g::AInst> host_inst;
   std::vector<int64_t> host_vox_off;
   hs2g::AInst* inst = nullptr;
@@ -650,16 +1012,50 @@ cudaError_t grow(double** p, int64_t* cap, int64_t need) {
   return e;
 }
 
+// line solves: the few-line kernels when the lines leave each SM about one warp (y, z) or two groups (x) and
+// fit in shared memory, else the register-blocked / fused ones (same bits either way)
+bool few_lines(const hs2g_adjoint* a, int axis) {
+  return line_threads(a->nlines[axis]) == 32 && a->max_len[axis] <= hs2g::kFewMaxLen;
+}
+bool few_x(const hs2g_adjoint* a) {
+  return a->nxgroups <= hs2g::kFewXGroups && a->max_len[0] <= hs2g::kFewMaxLen;
+}
+void ysolve(hs2g_adjoint* a, cudaStream_t st, int axis, const double* rhs, double* y, const double* T_in,
+            double* T_out) {
+  const hs2g::AView v = view(a);
+  const int64_t nl = a->nlines[axis];
+  if (few_lines(a, axis))
+    hs2g::adj_ysolve_few_kernel<<<line_blocks(nl), 32, hs2g::few_smem_bytes(a->max_len[axis]), st>>>(
+        v, axis, nl, a->max_len[axis], a->M, rhs, a->lo[axis], a->u[axis], a->ip[axis], y, T_in, T_out);
+  else
+    hs2g::adj_ysolve_kernel<<<line_blocks(nl), line_threads(nl), 0, st>>>(
+        v, axis, nl, a->M, rhs, a->lo[axis], a->u[axis], a->ip[axis], y, T_in, T_out);
+}
+void ysolve_t(hs2g_adjoint* a, cudaStream_t st, int axis, const double* M, const double* rhs, double* mu) {
+  const hs2g::AView v = view(a);
+  const int64_t nl = a->nlines[axis];
+  if (few_lines(a, axis))
+    hs2g::adj_ysolve_t_few_kernel<<<line_blocks(nl), 32, hs2g::few_smem_bytes(a->max_len[axis]), st>>>(
+        v, axis, nl, a->max_len[axis], M, rhs, a->lo[axis], a->u[axis], a->ip[axis], mu);
+  else
+    hs2g::adj_ysolve_t_kernel<<<line_blocks(nl), line_threads(nl), 0, st>>>(
+        v, axis, nl, M, rhs, a->lo[axis], a->u[axis], a->ip[axis], mu);
+}
+
 // one forward step T_in -> T_out on stream st keeping y0, y1, y2 (T_out may alias T_in; NULL skips it)
 cudaError_t fwd_step(hs2g_adjoint* a, cudaStream_t st, const double* T_in, double* T_out, double* y0, double* y1,
                      double* y2, double s) {
   const hs2g::AView v = view(a);
-  hs2g::adj_xfwd_kernel<<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(v, T_in, a->g[0], a->g[1], a->g[2], a->D, a->q, s,
-                                                                      a->lo[0], a->u[0], a->ip[0], y0);
-  hs2g::adj_ysolve_kernel<<<line_blocks(a->nlines[1]), line_threads(a->nlines[1]), 0, st>>>(
-      v, 1, a->nlines[1], a->M, y0, a->lo[1], a->u[1], a->ip[1], y1, nullptr, nullptr);
-  hs2g::adj_ysolve_kernel<<<line_blocks(a->nlines[2]), line_threads(a->nlines[2]), 0, st>>>(
-      v, 2, a->nlines[2], a->M, y1, a->lo[2], a->u[2], a->ip[2], y2, T_in, T_out);
+  if (few_x(a)) {
+    hs2g::adj_resid_kernel<<<nblk(a->n), kTh, 0, st>>>(v, T_in, a->g[0], a->g[1], a->g[2], a->D, a->q, s, y0);
+    hs2g::adj_xsolve_few_kernel<<<(unsigned)a->nxgroups, 128, hs2g::few_x_smem_bytes(a->max_len[0]), st>>>(
+        v, a->max_len[0], y0, a->lo[0], a->u[0], a->ip[0], y0);
+  } else {
+    hs2g::adj_xfwd_kernel<<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(v, T_in, a->g[0], a->g[1], a->g[2], a->D, a->q,
+                                                                        s, a->lo[0], a->u[0], a->ip[0], y0);
+  }
+  ysolve(a, st, 1, y0, y1, nullptr, nullptr);
+  ysolve(a, st, 2, y1, y2, T_in, T_out);
   return cudaGetLastError();
 }
 
@@ -668,12 +1064,14 @@ cudaError_t bwd_step(hs2g_adjoint* a, const double* Tn, const double* y0, const 
                      double s, int64_t obs_step) {
   const hs2g::AView v = view(a);
   cudaStream_t st = a->stream;
-  hs2g::adj_ysolve_t_kernel<<<line_blocks(a->nlines[2]), line_threads(a->nlines[2]), 0, st>>>(
-      v, 2, a->nlines[2], nullptr, a->lam, a->lo[2], a->u[2], a->ip[2], a->mu[2]);
-  hs2g::adj_ysolve_t_kernel<<<line_blocks(a->nlines[1]), line_threads(a->nlines[1]), 0, st>>>(
-      v, 1, a->nlines[1], a->M, a->mu[2], a->lo[1], a->u[1], a->ip[1], a->mu[1]);
-  hs2g::adj_xsolve_t_kernel<<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(v, a->M, a->mu[1], a->lo[0], a->u[0],
-                                                                          a->ip[0], a->mu[0]);
+  ysolve_t(a, st, 2, nullptr, a->lam, a->mu[2]);
+  ysolve_t(a, st, 1, a->M, a->mu[2], a->mu[1]);
+  if (few_x(a))
+    hs2g::adj_xsolve_t_few_kernel<<<(unsigned)a->nxgroups, 128, hs2g::few_x_smem_bytes(a->max_len[0]), st>>>(
+        v, a->max_len[0], a->M, a->mu[1], a->lo[0], a->u[0], a->ip[0], a->mu[0]);
+  else
+    hs2g::adj_xsolve_t_kernel<<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(v, a->M, a->mu[1], a->lo[0], a->u[0],
+                                                                            a->ip[0], a->mu[0]);
   hs2g::adj_update_kernel<<<nblk(a->n), kTh, 0, st>>>(v, a->g[0], a->g[1], a->g[2], Tn, y0, y1, y2, a->mu[0],
                                                       a->mu[1], a->mu[2], s, a->obs, obs_step, a->lam, a->gg[0],
                                                       a->gg[1], a->gg[2], a->gM, a->gq);
@@ -751,6 +1149,11 @@ int hs2g_adjoint_create(int n, const hs2g_adjoint_grid* grids, double dt, int de
   a->n = vox_off[n];
   a->nobs_step = nobs;
   for (int ax = 0; ax < 3; ++ax) a->nlines[ax] = line_off[ax * (n + 1) + n];
+  for (const auto& in : inst) {
+    a->max_len[0] = std::max(a->max_len[0], in.nx);
+    a->max_len[1] = std::max(a->max_len[1], in.ny);
+    a->max_len[2] = std::max(a->max_len[2], in.nz);
+  }
   a->nxgroups = xg_off[n];
   a->host_inst = inst;
   a->host_vox_off = vox_off;
@@ -763,6 +1166,18 @@ int hs2g_adjoint_create(int n, const hs2g_adjoint_grid* grids, double dt, int de
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&a->ev_done[b], cudaEventDisableTiming);
   }
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&a->ev_start, cudaEventDisableTiming);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(hs2g::adj_ysolve_few_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)hs2g::few_smem_bytes(hs2g::kFewMaxLen));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(hs2g::adj_ysolve_t_few_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)hs2g::few_smem_bytes(hs2g::kFewMaxLen));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(hs2g::adj_xsolve_few_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)hs2g::few_x_smem_bytes(hs2g::kFewMaxLen));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(hs2g::adj_xsolve_t_few_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)hs2g::few_x_smem_bytes(hs2g::kFewMaxLen));
   if (e == cudaSuccess) e = cudaMalloc(&a->inst, sizeof(hs2g::AInst) * n);
   if (e == cudaSuccess) e = cudaMalloc(&a->vox_off, sizeof(int64_t) * (n + 1));
   if (e == cudaSuccess) e = cudaMalloc(&a->line_off, sizeof(int64_t) * 3 * (n + 1));

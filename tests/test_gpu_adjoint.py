@@ -96,6 +96,27 @@ def test_batch_equals_single_instances(cuda_ok):
             np.testing.assert_array_equal(x[i], y)
 
 
+def test_batch_equals_single_instances_across_line_kernels(cuda_ok):
+    """The batch has enough y- and z-lines for the register-blocked line kernels; the instances run alone have
+    few enough for the shared-memory few-line kernels (y for all, z for the two smaller).  Both give the same
+    bits."""
+    dt, N = 0.005, 6
+    shapes = [(48, 144, 144), (48, 144, 144), (40, 100, 100), (30, 120, 160)]
+    probs = [_problem(40 + i, s, N) for i, s in enumerate(shapes)]
+    for p in probs[1:]:
+        p["schedule"] = probs[0]["schedule"]
+    b = Adjoint([(p["shape"], p["spacing"]) for p in probs], dt)
+    b.set_parameters([p["k"] for p in probs], [p["C"] for p in probs], [p["q"] for p in probs])
+    lb = b.forward([p["T0"] for p in probs], [p["obs"] for p in probs], probs[0]["schedule"], 3)
+    gb = b.backward()
+    for i, p in enumerate(probs):
+        a, la = _adjoint(p, dt, 3)
+        ga = a.backward()
+        assert lb[i] == la[0]
+        for x, y in zip(gb, ga):
+            np.testing.assert_array_equal(x[i], y)
+
+
 def _flash_problem(seed, shape, N, sp=(1e-3, 1e-3, 1e-3), dt=0.01):
     """A realistic inverse problem: lognormal k, flash in the top layer during the first step, observations
     from the semi-infinite-body response plus noise."""
