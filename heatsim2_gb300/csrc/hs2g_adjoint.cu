@@ -12,11 +12,8 @@
 //     dJ/dG_f (face q|p on axis a, q the lower voxel) += -(mu0_p - mu0_q)(T_p - T_q)
 //                                                       - (mu_a,p - mu_a,q)(y_a,p - y_a,q) / 2
 //     dJ/dM_p += mu2 y1 + mu1 y0 - mu0 y0 - mu1 y1 - mu2 y2,     dJ/dq_p += s_n mu0_p
-// with (mu_a, y_a) = (mu0, y0), (mu1, y1), (mu2, y2) for a = x, y, z (L is symmetric).  The transposed
-// tridiagonal solves reuse the forward factors: A = Lo U along a line (Lo: pivots piv_r on the diagonal,
-// lo_r below; U: unit diagonal, u_r above), so A^T x = b is  w_r = b_r - u_{r-1} w_{r-1}  (rows ascending)
-// then  x_r = (w_r - lo_{r+1} x_{r+1}) / piv_r  (rows descending): the forward solve's two passes, transposed
-// and swept in the opposite direction.
+// with (mu_a, y_a) = (mu0, y0), (mu1, y1), (mu2, y2) for a = x, y, z (L is symmetric).  A_a = M - L_a/2 is
+// symmetric too, so A_a^-T = A_a^-1: the adjoint's line solves are the forward ones, with the same factors.
 //
 // Memory: T is checkpointed every `ckpt` steps in the forward pass (ceil(nsteps/ckpt) states); the backward
 // pass recomputes a segment from its checkpoint, keeping T_n, y0, y1, y2 of each of its steps (4*ckpt states,
@@ -126,9 +123,10 @@ __global__ void adj_diag_kernel(AView v, const double* __restrict__ gx, const do
   D[p] = d;
 }
 
-// factors of A_a = M - L_a/2 per line: lo (sub-diagonal), u (normalised super-diagonal), ip (1/pivot)
+// factors of A_a = M - L_a/2 per line, kept in the form the one-FMA-per-row recurrences of the solves use:
+// e = lo / piv (lo the sub-diagonal), u = (super-diagonal) / piv, ip = 1 / piv
 __global__ void adj_factor_kernel(AView v, int axis, int64_t nlines, const double* __restrict__ M,
-                                  const double* __restrict__ g, double* __restrict__ lo, double* __restrict__ u,
+                                  const double* __restrict__ g, double* __restrict__ e, double* __restrict__ u,
                                   double* __restrict__ ip) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= nlines) return;
@@ -141,12 +139,21 @@ __global__ void adj_factor_kernel(AView v, int axis, int64_t nlines, const doubl
     const double l = -(0.5 * gl);
     const double piv = M[p] + 0.5 * (gl + gh) - u_prev * l;
     const double uu = -(0.5 * gh) / piv;
-    lo[p] = l;
+    const double inv = 1.0 / piv;
+    e[p] = l * inv;
     u[p] = uu;
-    ip[p] = 1.0 / piv;
+    ip[p] = inv;
     u_prev = uu;
   }
 }
+
+// Every line solve below is y = A_a^-1 b with A_a = Lo U (Lo: pivots on the diagonal, lo below; U: unit
+// diagonal, u above) in two passes of one dependent FMA per row:
+//     z_r = fma(-e_r, z_{r-1}, c_r),  c_r = b_r * ip_r     (rows ascending)
+//     y_r = fma(-u_r, y_{r+1}, z_r)                           (rows descending)
+// with b = M rhs (or rhs itself, or the residual r0 in the forward x stage).  The rounding of every operation
+// is explicit (no contraction left to the compiler), so the register-blocked kernels for many lines and the
+// shared-memory few-line kernels give the same bits.
 
 // The x-line kernels below stage 32 lines x 32 columns of each operand through shared memory: loads and
 // stores are row-contiguous (lane = column), the recurrence runs one line per lane of warp 0 (lane = line).
@@ -186,16 +193,17 @@ __device__ __forceinline__ double residual_at(const double* __restrict__ T, cons
   return r;
 }
 
-// forward x stage fused with the residual r0 = L T + s q: y0 = A_x^-1 r0, forward elimination
-// z_r = (r0_r - lo_r z_{r-1}) / piv_r, then back substitution y_r = z_r - u_r y_{r+1}
-__global__ void __launch_bounds__(kXT) adj_xfwd_kernel(AView v, const double* __restrict__ T,
-                                                       const double* __restrict__ gx, const double* __restrict__ gy,
-                                                       const double* __restrict__ gz, const double* __restrict__ D,
-                                                       const double* __restrict__ q, double s,
-                                                       const double* __restrict__ lo,
-                                                       const double* __restrict__ u, const double* __restrict__ ip,
-                                                       double* __restrict__ y0) {
-  __shared__ double sr[kXL][kXC + 1], sl[kXL][kXC + 1], si[kXL][kXC + 1];
+// x stage: y = A_x^-1 b.  RESID: b = the residual r0 = L T + s q (the forward step's first stage, fused);
+// otherwise b = M rhs (the adjoint's last stage, mu0 = A_x^-1 (M mu1)).
+template <bool RESID>
+__global__ void __launch_bounds__(kXT) adj_xsolve_kernel(AView v, const double* __restrict__ T,
+                                                         const double* __restrict__ gx, const double* __restrict__ gy,
+                                                         const double* __restrict__ gz, const double* __restrict__ D,
+                                                         const double* __restrict__ q, double s,
+                                                         const double* __restrict__ M, const double* __restrict__ rhs,
+                                                         const double* __restrict__ e, const double* __restrict__ u,
+                                                         const double* __restrict__ ip, double* __restrict__ y) {
+  __shared__ double sc[kXL][kXC + 1], se[kXL][kXC + 1];
   const XGroup g = xgroup(v, blockIdx.x);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr int kPer = kXL / (kXT / 32);
@@ -207,11 +215,15 @@ __global__ void __launch_bounds__(kXT) adj_xfwd_kernel(AView v, const double* __
     for (int ll = 0; ll < kPer; ++ll) {
       const int l = warp * kPer + ll;
       if (l < g.nl && i < g.nx) {
-        const int64_t line = g.l0 + l, j = line % g.ny, k = line / g.ny;
+        const int64_t line = g.l0 + l;
         const int64_t p = g.off + line * g.nx + i;
-        sr[l][lane] = residual_at(T, gx, gy, gz, D, q, s, p, i, j, k, g.nx, g.ny, g.nz);
-        sl[l][lane] = lo[p];
-        si[l][lane] = ip[p];
+        double b;
+        if (RESID)
+          b = residual_at(T, gx, gy, gz, D, q, s, p, i, line % g.ny, line / g.ny, g.nx, g.ny, g.nz);
+        else
+          b = __dmul_rn(M[p], rhs[p]);
+        sc[l][lane] = __dmul_rn(b, ip[p]);
+        se[l][lane] = e[p];
       }
     }
     __syncthreads();
@@ -219,15 +231,15 @@ __global__ void __launch_bounds__(kXT) adj_xfwd_kernel(AView v, const double* __
       const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
       double z = carry;
       for (int cc = 0; cc < cw; ++cc) {
-        z = __dmul_rn(__fma_rn(-sl[lane][cc], z, sr[lane][cc]), si[lane][cc]);
-        sr[lane][cc] = z;
+        z = __fma_rn(-se[lane][cc], z, sc[lane][cc]);
+        sc[lane][cc] = z;
       }
       carry = z;
     }
     __syncthreads();
     for (int ll = 0; ll < kPer; ++ll) {
       const int l = warp * kPer + ll;
-      if (l < g.nl && i < g.nx) y0[g.off + (g.l0 + l) * g.nx + i] = sr[l][lane];
+      if (l < g.nl && i < g.nx) y[g.off + (g.l0 + l) * g.nx + i] = sc[l][lane];
     }
     __syncthreads();
   }
@@ -238,8 +250,8 @@ __global__ void __launch_bounds__(kXT) adj_xfwd_kernel(AView v, const double* __
       const int l = warp * kPer + ll;
       if (l < g.nl && i < g.nx) {
         const int64_t p = g.off + (g.l0 + l) * g.nx + i;
-        sr[l][lane] = y0[p];
-        sl[l][lane] = u[p];
+        sc[l][lane] = y[p];
+        se[l][lane] = u[p];
       }
     }
     __syncthreads();
@@ -247,210 +259,91 @@ __global__ void __launch_bounds__(kXT) adj_xfwd_kernel(AView v, const double* __
       const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
       double x = carry;
       for (int cc = cw - 1; cc >= 0; --cc) {
-        x = __fma_rn(-sl[lane][cc], x, sr[lane][cc]);
-        sr[lane][cc] = x;
+        x = __fma_rn(-se[lane][cc], x, sc[lane][cc]);
+        sc[lane][cc] = x;
       }
       carry = x;
     }
     __syncthreads();
     for (int ll = 0; ll < kPer; ++ll) {
       const int l = warp * kPer + ll;
-      if (l < g.nl && i < g.nx) y0[g.off + (g.l0 + l) * g.nx + i] = sr[l][lane];
+      if (l < g.nl && i < g.nx) y[g.off + (g.l0 + l) * g.nx + i] = sc[l][lane];
     }
     __syncthreads();
   }
 }
 
-// transposed x stage: mu0 = A_x^-T (M mu1), the arithmetic of adj_solve_t_kernel on axis 0
-__global__ void __launch_bounds__(kXT) adj_xsolve_t_kernel(AView v, const double* __restrict__ M,
-                                                           const double* __restrict__ rhs,
-                                                           const double* __restrict__ lo,
-                                                           const double* __restrict__ u,
-                                                           const double* __restrict__ ip, double* __restrict__ mu) {
-  __shared__ double sb[kXL][kXC + 1], sl[kXL][kXC + 1], si[kXL][kXC + 1];
-  const XGroup g = xgroup(v, blockIdx.x);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  constexpr int kPer = kXL / (kXT / 32);
-  const int nch = (int)((g.nx + kXC - 1) / kXC);
-  double w = 0.0, u_prev = 0.0;
-  for (int ch = 0; ch < nch; ++ch) {  // U^T w = M rhs, rows ascending
-    const int64_t i = (int64_t)ch * kXC + lane;
-    for (int ll = 0; ll < kPer; ++ll) {
-      const int l = warp * kPer + ll;
-      if (l < g.nl && i < g.nx) {
-        const int64_t p = g.off + (g.l0 + l) * g.nx + i;
-        sb[l][lane] = __dmul_rn(M[p], rhs[p]);
-        sl[l][lane] = u[p];
-      }
-    }
-    __syncthreads();
-    if (warp == 0 && lane < g.nl) {
-      const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
-      for (int cc = 0; cc < cw; ++cc) {
-        w = __fma_rn(-u_prev, w, sb[lane][cc]);
-        u_prev = sl[lane][cc];
-        sb[lane][cc] = w;
-      }
-    }
-    __syncthreads();
-    for (int ll = 0; ll < kPer; ++ll) {
-      const int l = warp * kPer + ll;
-      if (l < g.nl && i < g.nx) mu[g.off + (g.l0 + l) * g.nx + i] = sb[l][lane];
-    }
-    __syncthreads();
-  }
-  double x = 0.0, lo_next = 0.0;
-  for (int ch = nch - 1; ch >= 0; --ch) {  // Lo^T x = w, rows descending
-    const int64_t i = (int64_t)ch * kXC + lane;
-    for (int ll = 0; ll < kPer; ++ll) {
-      const int l = warp * kPer + ll;
-      if (l < g.nl && i < g.nx) {
-        const int64_t p = g.off + (g.l0 + l) * g.nx + i;
-        sb[l][lane] = mu[p];
-        sl[l][lane] = lo[p];
-        si[l][lane] = ip[p];
-      }
-    }
-    __syncthreads();
-    if (warp == 0 && lane < g.nl) {
-      const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
-      for (int cc = cw - 1; cc >= 0; --cc) {
-        x = __dmul_rn(__fma_rn(-lo_next, x, sb[lane][cc]), si[lane][cc]);
-        lo_next = sl[lane][cc];
-        sb[lane][cc] = x;
-      }
-    }
-    __syncthreads();
-    for (int ll = 0; ll < kPer; ++ll) {
-      const int l = warp * kPer + ll;
-      if (l < g.nl && i < g.nx) mu[g.off + (g.l0 + l) * g.nx + i] = sb[l][lane];
-    }
-    __syncthreads();
-  }
-}
-
-// y / z stage, forward: y = A_a^-1 (M rhs) along each strided line (one thread per line, neighbouring
-// threads on neighbouring lines, so every row access is coalesced); T_out = T_in + y when T_out is given.
-// Rows go in blocks of kRB: the loads of a block are issued together, then the recurrence runs through it,
-// so a line pays one memory latency per block instead of one per row.  The rounding of every operation is
-// explicit (no contraction left to the compiler) so that the few-line kernels below, which stage rows
-// differently, give the same bits.
+// y / z stage: y = A_a^-1 (M rhs) along each strided line (M null: A_a^-1 rhs), one thread per line,
+// neighbouring threads on neighbouring lines, so every row access is coalesced; T_out = T_in + y when T_out
+// is given (T_out may equal T_in).  Rows go in blocks of kRB: the loads of a block are issued together, then
+// the recurrence runs through it, so a line pays one memory latency per block instead of one per row.
 constexpr int kRB = 8;
 
-__global__ void __launch_bounds__(128, 4) adj_ysolve_kernel(AView v, int axis, int64_t nlines, const double* __restrict__ M,
-                                  const double* __restrict__ rhs, const double* __restrict__ lo,
-                                  const double* __restrict__ u, const double* __restrict__ ip,
-                                  double* __restrict__ y, const double* __restrict__ T_in,
-                                  double* __restrict__ T_out) {
+template <bool HAS_M, bool ADD_T>
+__global__ void __launch_bounds__(128, 4) adj_ysolve_kernel(AView v, int axis, int64_t nlines,
+                                                            const double* __restrict__ M, const double* rhs,
+                                                            const double* __restrict__ e,
+                                                            const double* __restrict__ u,
+                                                            const double* __restrict__ ip, double* y,
+                                                            const double* T_in, double* T_out) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= nlines) return;
   const Line ln = line_at(v, axis, t);
   double z = 0.0;
   for (int64_t r0 = 0; r0 < ln.len; r0 += kRB) {
-    double b[kRB], l[kRB], iv[kRB];
+    double c[kRB], ee[kRB];
 #pragma unroll
-    for (int e = 0; e < kRB; ++e) {
-      if (r0 + e < ln.len) {
-        const int64_t p = ln.base + (r0 + e) * ln.stride;
-        b[e] = __dmul_rn(M[p], rhs[p]);
-        l[e] = lo[p];
-        iv[e] = ip[p];
+    for (int k = 0; k < kRB; ++k) {
+      if (r0 + k < ln.len) {
+        const int64_t p = ln.base + (r0 + k) * ln.stride;
+        const double b = HAS_M ? __dmul_rn(M[p], rhs[p]) : rhs[p];
+        c[k] = __dmul_rn(b, ip[p]);
+        ee[k] = e[p];
       }
     }
 #pragma unroll
-    for (int e = 0; e < kRB; ++e) {
-      if (r0 + e < ln.len) {
-        z = __dmul_rn(__fma_rn(-l[e], z, b[e]), iv[e]);
-        y[ln.base + (r0 + e) * ln.stride] = z;
+    for (int k = 0; k < kRB; ++k) {
+      if (r0 + k < ln.len) {
+        z = __fma_rn(-ee[k], z, c[k]);
+        y[ln.base + (r0 + k) * ln.stride] = z;
       }
     }
   }
   double x = 0.0;
   for (int64_t r1 = ln.len - 1; r1 >= 0; r1 -= kRB) {
-    double yy[kRB], uu[kRB], tt[kRB];
+    double yy[kRB], uu[kRB], tt[kRB] = {};
 #pragma unroll
-    for (int e = 0; e < kRB; ++e) {
-      if (r1 - e >= 0) {
-        const int64_t p = ln.base + (r1 - e) * ln.stride;
-        yy[e] = y[p];
-        uu[e] = u[p];
-        tt[e] = T_out ? T_in[p] : 0.0;
+    for (int k = 0; k < kRB; ++k) {
+      if (r1 - k >= 0) {
+        const int64_t p = ln.base + (r1 - k) * ln.stride;
+        yy[k] = y[p];
+        uu[k] = u[p];
+        if (ADD_T) tt[k] = T_in[p];
       }
     }
 #pragma unroll
-    for (int e = 0; e < kRB; ++e) {
-      if (r1 - e >= 0) {
-        const int64_t p = ln.base + (r1 - e) * ln.stride;
-        x = __fma_rn(-uu[e], x, yy[e]);
+    for (int k = 0; k < kRB; ++k) {
+      if (r1 - k >= 0) {
+        const int64_t p = ln.base + (r1 - k) * ln.stride;
+        x = __fma_rn(-uu[k], x, yy[k]);
         y[p] = x;
-        if (T_out) T_out[p] = __dadd_rn(tt[e], x);
+        if (ADD_T) T_out[p] = __dadd_rn(tt[k], x);
       }
     }
   }
 }
 
-// y / z stage, transposed: mu = A_a^-T (scale * rhs) along each strided line (scale = M, or 1 when M is
-// null), rows in blocks of kRB as above
-__global__ void __launch_bounds__(128, 4) adj_ysolve_t_kernel(AView v, int axis, int64_t nlines, const double* __restrict__ M,
-                                    const double* __restrict__ rhs, const double* __restrict__ lo,
-                                    const double* __restrict__ u, const double* __restrict__ ip,
-                                    double* __restrict__ mu) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= nlines) return;
-  const Line ln = line_at(v, axis, t);
-  double w = 0.0, u_prev = 0.0;
-  for (int64_t r0 = 0; r0 < ln.len; r0 += kRB) {  // U^T w = b, rows ascending
-    double b[kRB], uu[kRB];
-#pragma unroll
-    for (int e = 0; e < kRB; ++e) {
-      if (r0 + e < ln.len) {
-        const int64_t p = ln.base + (r0 + e) * ln.stride;
-        b[e] = M ? __dmul_rn(M[p], rhs[p]) : rhs[p];
-        uu[e] = u[p];
-      }
-    }
-#pragma unroll
-    for (int e = 0; e < kRB; ++e) {
-      if (r0 + e < ln.len) {
-        w = __fma_rn(-u_prev, w, b[e]);
-        u_prev = uu[e];
-        mu[ln.base + (r0 + e) * ln.stride] = w;
-      }
-    }
-  }
-  double x = 0.0, lo_next = 0.0;
-  for (int64_t r1 = ln.len - 1; r1 >= 0; r1 -= kRB) {  // Lo^T x = w, rows descending
-    double ww[kRB], l[kRB], iv[kRB];
-#pragma unroll
-    for (int e = 0; e < kRB; ++e) {
-      if (r1 - e >= 0) {
-        const int64_t p = ln.base + (r1 - e) * ln.stride;
-        ww[e] = mu[p];
-        l[e] = lo[p];
-        iv[e] = ip[p];
-      }
-    }
-#pragma unroll
-    for (int e = 0; e < kRB; ++e) {
-      if (r1 - e >= 0) {
-        x = __dmul_rn(__fma_rn(-lo_next, x, ww[e]), iv[e]);
-        lo_next = l[e];
-        mu[ln.base + (r1 - e) * ln.stride] = x;
-      }
-    }
-  }
-}
-
-// Few-line forms of the two kernels above.  A small problem (4096 y-lines of 128 rows at 32x128x128) leaves
-// each SM about one warp, whose line is then a chain of memory round trips, one per block of rows.  Here a
+// Few-line form of adj_ysolve_kernel.  A small problem (4096 y-lines of 128 rows at 32x128x128) leaves each
+// SM about one warp, whose line is then a chain of memory round trips, one per block of rows.  Here a
 // 32-thread CTA streams its lines' rows through a ring of kFS stages of kFR rows with cp.async (each thread
 // copies its own line's elements, so no barrier is needed), keeping up to (kFS - 1) * kFR rows in flight, and
 // holds the first pass's values of the whole line in shared memory for the second pass.  Same operations,
-// same order, same rounding as adj_ysolve_kernel / adj_ysolve_t_kernel.
-// What remains is the FP64 chain: GB300 issues a warp's FP64 instruction over ~60 cycles of its
-// sub-partition's pipe whatever the number of active lanes (0.54 lanes per clock), so a 128-row line of the
-// five-operation forward solve takes ~20 us however the lines are spread over warps (measured: four 8-lane
-// warps per 32 lines gave the same y time and doubled the z time).
+// same order, same rounding as adj_ysolve_kernel.
+// What bounds it is the lone warp's own instruction stream (about 6 cycles per instruction with nothing to
+// interleave), not memory: at 32x128x128 the 128-row y solve takes 38 us, 26 us of it with the copies left out
+// (a timing probe); eight ring stages or 16-row stages were slower, and staging each block's operands in
+// registers changed nothing.  Spreading the lines over four 8-lane warps gave the same y time and doubled the
+// z time.
 constexpr int kFS = 4;            // ring stages
 constexpr int kFR = 8;            // rows per stage
 constexpr int kFewMaxLen = 512;   // longest line the few-line kernels hold (128 KB of line values)
@@ -464,27 +357,24 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
-__device__ __forceinline__ void cp_async_wait_ring() { cp_async_wait<kFS - 1>(); }
 
 // dynamic shared memory of a few-line launch: the line values, then the ring of up to 4 operands
 inline size_t few_smem_bytes(int64_t max_len) {
   return sizeof(double) * 32 * (size_t)(max_len + kFS * kFR * 4);
 }
 
-// Streams `nops` operands of rows r(g, e) of block g into ring slot g % kFS; rows outside the line are skipped.
-// Always commits a group, so that exactly kFS - 1 groups are younger than the one the consumer waits for.
+// slot of operand a of row k of block g in the ring (block g in slot g % kFS)
 struct FewRing {
   double* ring;
   int lane;
-  __device__ __forceinline__ double* at(int g, int e, int a) const {
-    return ring + (((g % kFS) * kFR + e) * 4 + a) * 32 + lane;
+  __device__ __forceinline__ double* at(int g, int k, int a) const {
+    return ring + (((g % kFS) * kFR + k) * 4 + a) * 32 + lane;
   }
 };
 
 __global__ void __launch_bounds__(32) adj_ysolve_few_kernel(AView v, int axis, int64_t nlines, int64_t max_len,
-                                                            const double* __restrict__ M,
-                                                            const double* __restrict__ rhs,
-                                                            const double* __restrict__ lo,
+                                                            const double* __restrict__ M, const double* rhs,
+                                                            const double* __restrict__ e,
                                                             const double* __restrict__ u,
                                                             const double* __restrict__ ip, double* y,
                                                             const double* T_in, double* T_out) {
@@ -496,146 +386,79 @@ __global__ void __launch_bounds__(32) adj_ysolve_few_kernel(AView v, int axis, i
   double* line = few_sm;  // line[r * 32 + lane]
   const FewRing R{few_sm + 32 * max_len, lane};
   const int len = (int)ln.len, nb = (len + kFR - 1) / kFR;
-  auto issue_fwd = [&](int g) {
+  // every issue commits a group (empty past the line's end), so exactly kFS - 1 groups are younger than the
+  // one waited for
+  auto issue_asc = [&](int g) {
     if (g < nb)
-      for (int e = 0; e < kFR; ++e) {
-        const int r = g * kFR + e;
+      for (int k = 0; k < kFR; ++k) {
+        const int r = g * kFR + k;
         if (r < len) {
           const int64_t p = ln.base + r * ln.stride;
-          cp_async8(R.at(g, e, 0), M + p);
-          cp_async8(R.at(g, e, 1), rhs + p);
-          cp_async8(R.at(g, e, 2), lo + p);
-          cp_async8(R.at(g, e, 3), ip + p);
-        }
-      }
-    cp_async_commit();
-  };
-  for (int g = 0; g < kFS - 1; ++g) issue_fwd(g);
-  double z = 0.0;
-  for (int g = 0; g < nb; ++g) {
-    issue_fwd(g + kFS - 1);  // into the slot consumed in the previous iteration
-    cp_async_wait_ring();
-    for (int e = 0; e < kFR; ++e) {
-      const int r = g * kFR + e;
-      if (r < len) {
-        const double b = __dmul_rn(*R.at(g, e, 0), *R.at(g, e, 1));
-        z = __dmul_rn(__fma_rn(-*R.at(g, e, 2), z, b), *R.at(g, e, 3));
-        line[r * 32 + lane] = z;
-      }
-    }
-  }
-  auto issue_bwd = [&](int g) {
-    if (g < nb)
-      for (int e = 0; e < kFR; ++e) {
-        const int r = len - 1 - (g * kFR + e);
-        if (r >= 0) {
-          const int64_t p = ln.base + r * ln.stride;
-          cp_async8(R.at(g, e, 0), u + p);
-          if (T_out) cp_async8(R.at(g, e, 1), T_in + p);
-        }
-      }
-    cp_async_commit();
-  };
-  for (int g = 0; g < kFS - 1; ++g) issue_bwd(g);
-  double x = 0.0;
-  for (int g = 0; g < nb; ++g) {
-    issue_bwd(g + kFS - 1);
-    cp_async_wait_ring();
-    for (int e = 0; e < kFR; ++e) {
-      const int r = len - 1 - (g * kFR + e);
-      if (r >= 0) {
-        const int64_t p = ln.base + r * ln.stride;
-        x = __fma_rn(-*R.at(g, e, 0), x, line[r * 32 + lane]);
-        y[p] = x;
-        if (T_out) T_out[p] = __dadd_rn(*R.at(g, e, 1), x);
-      }
-    }
-  }
-}
-
-__global__ void __launch_bounds__(32) adj_ysolve_t_few_kernel(AView v, int axis, int64_t nlines, int64_t max_len,
-                                                              const double* __restrict__ M,
-                                                              const double* __restrict__ rhs,
-                                                              const double* __restrict__ lo,
-                                                              const double* __restrict__ u,
-                                                              const double* __restrict__ ip,
-                                                              double* __restrict__ mu) {
-  extern __shared__ double few_sm[];
-  const int lane = threadIdx.x;
-  const int64_t t = blockIdx.x * (int64_t)32 + lane;
-  if (t >= nlines) return;
-  const Line ln = line_at(v, axis, t);
-  double* line = few_sm;
-  const FewRing R{few_sm + 32 * max_len, lane};
-  const int len = (int)ln.len, nb = (len + kFR - 1) / kFR;
-  auto issue_asc = [&](int g) {  // U^T w = b, rows ascending
-    if (g < nb)
-      for (int e = 0; e < kFR; ++e) {
-        const int r = g * kFR + e;
-        if (r < len) {
-          const int64_t p = ln.base + r * ln.stride;
-          cp_async8(R.at(g, e, 0), rhs + p);
-          cp_async8(R.at(g, e, 1), u + p);
-          if (M) cp_async8(R.at(g, e, 2), M + p);
+          cp_async8(R.at(g, k, 0), rhs + p);
+          cp_async8(R.at(g, k, 1), e + p);
+          cp_async8(R.at(g, k, 2), ip + p);
+          if (M) cp_async8(R.at(g, k, 3), M + p);
         }
       }
     cp_async_commit();
   };
   for (int g = 0; g < kFS - 1; ++g) issue_asc(g);
-  double w = 0.0, u_prev = 0.0;
+  double z = 0.0;
   for (int g = 0; g < nb; ++g) {
-    issue_asc(g + kFS - 1);
-    cp_async_wait_ring();
-    for (int e = 0; e < kFR; ++e) {
-      const int r = g * kFR + e;
+    issue_asc(g + kFS - 1);  // into the slot consumed in the previous iteration
+    cp_async_wait<kFS - 1>();
+    for (int k = 0; k < kFR; ++k) {
+      const int r = g * kFR + k;
       if (r < len) {
-        const double b = M ? __dmul_rn(*R.at(g, e, 2), *R.at(g, e, 0)) : *R.at(g, e, 0);
-        w = __fma_rn(-u_prev, w, b);
-        u_prev = *R.at(g, e, 1);
-        line[r * 32 + lane] = w;
+        const double b = M ? __dmul_rn(*R.at(g, k, 3), *R.at(g, k, 0)) : *R.at(g, k, 0);
+        z = __fma_rn(-*R.at(g, k, 1), z, __dmul_rn(b, *R.at(g, k, 2)));
+        line[r * 32 + lane] = z;
       }
     }
   }
-  auto issue_desc = [&](int g) {  // Lo^T x = w, rows descending
+  auto issue_desc = [&](int g) {
     if (g < nb)
-      for (int e = 0; e < kFR; ++e) {
-        const int r = len - 1 - (g * kFR + e);
+      for (int k = 0; k < kFR; ++k) {
+        const int r = len - 1 - (g * kFR + k);
         if (r >= 0) {
           const int64_t p = ln.base + r * ln.stride;
-          cp_async8(R.at(g, e, 0), lo + p);
-          cp_async8(R.at(g, e, 1), ip + p);
+          cp_async8(R.at(g, k, 0), u + p);
+          if (T_out) cp_async8(R.at(g, k, 1), T_in + p);
         }
       }
     cp_async_commit();
   };
   for (int g = 0; g < kFS - 1; ++g) issue_desc(g);
-  double x = 0.0, lo_next = 0.0;
+  double x = 0.0;
   for (int g = 0; g < nb; ++g) {
     issue_desc(g + kFS - 1);
-    cp_async_wait_ring();
-    for (int e = 0; e < kFR; ++e) {
-      const int r = len - 1 - (g * kFR + e);
+    cp_async_wait<kFS - 1>();
+    for (int k = 0; k < kFR; ++k) {
+      const int r = len - 1 - (g * kFR + k);
       if (r >= 0) {
-        x = __dmul_rn(__fma_rn(-lo_next, x, line[r * 32 + lane]), *R.at(g, e, 1));
-        lo_next = *R.at(g, e, 0);
-        mu[ln.base + r * ln.stride] = x;
+        const int64_t p = ln.base + r * ln.stride;
+        x = __fma_rn(-*R.at(g, k, 0), x, line[r * 32 + lane]);
+        y[p] = x;
+        if (T_out) T_out[p] = __dadd_rn(*R.at(g, k, 1), x);
       }
     }
   }
 }
 
-// Few-line forms of the x stages.  A 32-line group of a small problem is a latency chain in
-// adj_xfwd_kernel (four dependent load rounds per 32-column chunk); here each of four warps streams the
-// chunks of kFewLanes of the group's lines through a ring of kXFS tiles with cp.async (lane = column,
-// row-contiguous copies), recurs with lane = line while the next two chunks are in flight, keeps the whole
-// lines in shared memory between the two passes and stores them once, row-contiguous.  The residual r0 comes from adj_resid_kernel (one thread per voxel)
-// instead of being fused.  Same operations, same order, same rounding as the fused kernels.
-constexpr int kXFS = 3;              // ring stages (tiles of kXL lines x kXC columns x 3 operands)
+// Few-line form of adj_xsolve_kernel.  A 32-line group of a small problem is a latency chain in the fused
+// kernel (four dependent load rounds per 32-column chunk); here each of four warps streams the chunks of
+// kFewLanes of the group's lines through a ring of kXFS tiles with cp.async (lane = column, row-contiguous
+// copies), recurs with lane = line while the next two chunks are in flight, keeps the whole lines in shared
+// memory between the two passes and stores them once, row-contiguous.  The forward stage's residual r0 comes
+// from adj_resid_kernel (one thread per voxel) instead of being fused.  Same operations, same order, same
+// rounding as adj_xsolve_kernel.
+constexpr int kXFS = 3;              // ring stages (tiles of kXL lines x kXC columns x up to 4 operands)
 constexpr int kFewLanes = 8;         // lines per warp (four warps per group: the copies spread over them)
-constexpr int kFewXGroups = 2 * 152; // at most this many 32-line groups (two CTAs per SM at 128 columns)
+constexpr int kFewXGroups = 2 * 152; // at most this many 32-line groups
+constexpr int kFewMaxNx = 448;       // longest x-line the few-line kernel holds (4 operands: 211 KB)
 
-inline size_t few_x_smem_bytes(int64_t max_nx) {
-  return sizeof(double) * ((size_t)kXL * (size_t)(max_nx + 1) + (size_t)kXFS * 3 * kXL * (kXC + 1));
+inline size_t few_x_smem_bytes(int64_t max_nx, int nops) {
+  return sizeof(double) * ((size_t)kXL * (size_t)(max_nx + 1) + (size_t)kXFS * nops * kXL * (kXC + 1));
 }
 
 __global__ void adj_resid_kernel(AView v, const double* __restrict__ T, const double* __restrict__ gx,
@@ -648,20 +471,23 @@ __global__ void adj_resid_kernel(AView v, const double* __restrict__ T, const do
   r0[p] = residual_at(T, gx, gy, gz, D, q, s, p, x.i, x.j, x.k, x.nx, x.ny, x.nz);
 }
 
-// the group's tiles and line buffer in dynamic shared memory: lines[l * (max_nx + 1) + c], then the ring
+// the group's line buffer and tiles in dynamic shared memory: lines[l * (max_nx + 1) + c], then the ring of
+// kXFS slots of nops operand tiles
 struct FewX {
   double* lines;
   double* ring;
   int64_t zs;
+  int nops;
   __device__ __forceinline__ double* tile(int seq, int a, int l) const {
-    return ring + (((seq % kXFS) * 3 + a) * kXL + l) * (kXC + 1);
+    return ring + (((seq % kXFS) * nops + a) * kXL + l) * (kXC + 1);
   }
 };
 
-// copies columns [ch * kXC, ch * kXC + kXC) of the group's lines of up to three operands into ring slot
-// seq % kXFS (nothing when ch is outside the line); always commits a group
+// copies columns [ch * kXC, ch * kXC + kXC) of the group's lines [l_begin, l_end) of the given operands (null
+// ones skipped) into ring slot seq % kXFS (nothing when ch is outside the line); always commits a group
 __device__ __forceinline__ void few_x_issue(const FewX& F, const XGroup& g, int seq, int ch, int lane, int l_begin,
-                                            int l_end, const double* a0, const double* a1, const double* a2) {
+                                            int l_end, const double* a0, const double* a1, const double* a2,
+                                            const double* a3) {
   const int64_t c = (int64_t)ch * kXC + lane;
   if (ch >= 0 && c < g.nx) {
     const int64_t row0 = g.off + g.l0 * g.nx + c;
@@ -670,55 +496,51 @@ __device__ __forceinline__ void few_x_issue(const FewX& F, const XGroup& g, int 
       cp_async8(F.tile(seq, 0, l) + lane, a0 + p);
       if (a1) cp_async8(F.tile(seq, 1, l) + lane, a1 + p);
       if (a2) cp_async8(F.tile(seq, 2, l) + lane, a2 + p);
+      if (a3) cp_async8(F.tile(seq, 3, l) + lane, a3 + p);
     }
   }
   cp_async_commit();
 }
 
-// the group's lines from the line buffer to global memory, row-contiguous
-__device__ __forceinline__ void few_x_store(const FewX& F, const XGroup& g, int lane, int l_begin, int l_end,
-                                            double* out) {
-  __syncwarp();
-  for (int l = l_begin; l < l_end; ++l)
-    for (int64_t c = lane; c < g.nx; c += 32) out[g.off + (g.l0 + l) * g.nx + c] = F.lines[l * F.zs + c];
-}
-
-// y0 = A_x^-1 r0 (r0 may alias y0), the arithmetic of adj_xfwd_kernel
-__global__ void __launch_bounds__(128) adj_xsolve_few_kernel(AView v, int64_t max_nx, const double* r0,
-                                                            const double* __restrict__ lo,
-                                                            const double* __restrict__ u,
-                                                            const double* __restrict__ ip, double* y0) {
+// y = A_x^-1 (M rhs), or A_x^-1 rhs when M is null (rhs = r0 in the forward stage; rhs may alias y)
+__global__ void __launch_bounds__(128) adj_xsolve_few_kernel(AView v, int64_t max_nx, const double* __restrict__ M,
+                                                             const double* rhs, const double* __restrict__ e,
+                                                             const double* __restrict__ u,
+                                                             const double* __restrict__ ip, double* y) {
   extern __shared__ double few_sm[];
   const XGroup g = xgroup(v, blockIdx.x);
   // warp w solves the group's lines [lb, le): it copies them with lane = column and recurs with lane = line
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int lb = min(warp * kFewLanes, (int)g.nl), le = min(lb + kFewLanes, (int)g.nl), ln = lb + lane;
-  const FewX F{few_sm, few_sm + kXL * (max_nx + 1), max_nx + 1};
+  const FewX F{few_sm, few_sm + kXL * (max_nx + 1), max_nx + 1, M ? 4 : 3};
   const int nch = (int)((g.nx + kXC - 1) / kXC);
-  for (int q = 0; q < kXFS - 1; ++q) few_x_issue(F, g, q, q < nch ? q : -1, lane, lb, le, r0, lo, ip);
+  for (int q = 0; q < kXFS - 1; ++q) few_x_issue(F, g, q, q < nch ? q : -1, lane, lb, le, rhs, e, ip, M);
   double z = 0.0;
   for (int ch = 0; ch < nch; ++ch) {
     __syncwarp();  // every lane is done with the slot refilled here
     const int nxt = ch + kXFS - 1;
-    few_x_issue(F, g, nxt, nxt < nch ? nxt : -1, lane, lb, le, r0, lo, ip);
+    few_x_issue(F, g, nxt, nxt < nch ? nxt : -1, lane, lb, le, rhs, e, ip, M);
     cp_async_wait<kXFS - 1>();
     __syncwarp();  // chunk ch's copies by every lane are visible
     if (ln < le) {
       const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
-      const double *tr = F.tile(ch, 0, ln), *tl = F.tile(ch, 1, ln), *ti = F.tile(ch, 2, ln);
+      const double *tb = F.tile(ch, 0, ln), *te = F.tile(ch, 1, ln), *ti = F.tile(ch, 2, ln);
+      const double* tm = M ? F.tile(ch, 3, ln) : tb;
       double* zr = F.lines + ln * F.zs + ch * kXC;
       for (int cc = 0; cc < cw; ++cc) {
-        z = __dmul_rn(__fma_rn(-tl[cc], z, tr[cc]), ti[cc]);
+        const double b = M ? __dmul_rn(tm[cc], tb[cc]) : tb[cc];
+        z = __fma_rn(-te[cc], z, __dmul_rn(b, ti[cc]));
         zr[cc] = z;
       }
     }
   }
   __syncwarp();
-  for (int q = 0; q < kXFS - 1; ++q) few_x_issue(F, g, q, nch - 1 - q, lane, lb, le, u, nullptr, nullptr);
+  for (int q = 0; q < kXFS - 1; ++q)
+    few_x_issue(F, g, q, nch - 1 - q, lane, lb, le, u, nullptr, nullptr, nullptr);
   double x = 0.0;
   for (int q = 0; q < nch; ++q) {
     __syncwarp();
-    few_x_issue(F, g, q + kXFS - 1, nch - kXFS - q, lane, lb, le, u, nullptr, nullptr);
+    few_x_issue(F, g, q + kXFS - 1, nch - kXFS - q, lane, lb, le, u, nullptr, nullptr, nullptr);
     cp_async_wait<kXFS - 1>();
     __syncwarp();
     const int ch = nch - 1 - q;
@@ -732,64 +554,9 @@ __global__ void __launch_bounds__(128) adj_xsolve_few_kernel(AView v, int64_t ma
       }
     }
   }
-  few_x_store(F, g, lane, lb, le, y0);
-}
-
-// mu = A_x^-T (M rhs), the arithmetic of adj_xsolve_t_kernel
-__global__ void __launch_bounds__(128) adj_xsolve_t_few_kernel(AView v, int64_t max_nx,
-                                                              const double* __restrict__ M,
-                                                              const double* __restrict__ rhs,
-                                                              const double* __restrict__ lo,
-                                                              const double* __restrict__ u,
-                                                              const double* __restrict__ ip,
-                                                              double* __restrict__ mu) {
-  extern __shared__ double few_sm[];
-  const XGroup g = xgroup(v, blockIdx.x);
-  // warp w solves the group's lines [lb, le): it copies them with lane = column and recurs with lane = line
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int lb = min(warp * kFewLanes, (int)g.nl), le = min(lb + kFewLanes, (int)g.nl), ln = lb + lane;
-  const FewX F{few_sm, few_sm + kXL * (max_nx + 1), max_nx + 1};
-  const int nch = (int)((g.nx + kXC - 1) / kXC);
-  for (int q = 0; q < kXFS - 1; ++q) few_x_issue(F, g, q, q < nch ? q : -1, lane, lb, le, rhs, M, u);
-  double w = 0.0, u_prev = 0.0;
-  for (int ch = 0; ch < nch; ++ch) {  // U^T w = M rhs, rows ascending
-    __syncwarp();
-    const int nxt = ch + kXFS - 1;
-    few_x_issue(F, g, nxt, nxt < nch ? nxt : -1, lane, lb, le, rhs, M, u);
-    cp_async_wait<kXFS - 1>();
-    __syncwarp();
-    if (ln < le) {
-      const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
-      const double *tb = F.tile(ch, 0, ln), *tm = F.tile(ch, 1, ln), *tu = F.tile(ch, 2, ln);
-      double* zr = F.lines + ln * F.zs + ch * kXC;
-      for (int cc = 0; cc < cw; ++cc) {
-        w = __fma_rn(-u_prev, w, __dmul_rn(tm[cc], tb[cc]));
-        u_prev = tu[cc];
-        zr[cc] = w;
-      }
-    }
-  }
   __syncwarp();
-  for (int q = 0; q < kXFS - 1; ++q) few_x_issue(F, g, q, nch - 1 - q, lane, lb, le, lo, ip, nullptr);
-  double x = 0.0, lo_next = 0.0;
-  for (int q = 0; q < nch; ++q) {  // Lo^T x = w, rows descending
-    __syncwarp();
-    few_x_issue(F, g, q + kXFS - 1, nch - kXFS - q, lane, lb, le, lo, ip, nullptr);
-    cp_async_wait<kXFS - 1>();
-    __syncwarp();
-    const int ch = nch - 1 - q;
-    if (ln < le) {
-      const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
-      const double *tl = F.tile(q, 0, ln), *ti = F.tile(q, 1, ln);
-      double* zr = F.lines + ln * F.zs + ch * kXC;
-      for (int cc = cw - 1; cc >= 0; --cc) {
-        x = __dmul_rn(__fma_rn(-lo_next, x, zr[cc]), ti[cc]);
-        lo_next = tl[cc];
-        zr[cc] = x;
-      }
-    }
-  }
-  few_x_store(F, g, lane, lb, le, mu);
+  for (int l = lb; l < le; ++l)
+    for (int64_t c = lane; c < g.nx; c += 32) y[g.off + (g.l0 + l) * g.nx + c] = F.lines[l * F.zs + c];
 }
 
 // lambda = misfit gradient of the last observation, 2 (T_N - d_{N-1}) on the top layer, 0 below
@@ -940,7 +707,8 @@ struct hs2g_adjoint {
   // parameters and derived fields
   double *k = nullptr, *C = nullptr, *q = nullptr, *M = nullptr, *D = nullptr;
   double* g[3] = {nullptr, nullptr, nullptr};
-  double *lo[3] = {nullptr, nullptr, nullptr}, *u[3] = {nullptr, nullptr, nullptr},
+  // line factors of A_x, A_y, A_z: e = lo / piv, u = super-diagonal / piv, ip = 1 / piv
+  double *e[3] = {nullptr, nullptr, nullptr}, *u[3] = {nullptr, nullptr, nullptr},
          *ip[3] = {nullptr, nullptr, nullptr};
   // run state
   bool have_params = false;
@@ -1018,28 +786,32 @@ bool few_lines(const hs2g_adjoint* a, int axis) {
   return line_threads(a->nlines[axis]) == 32 && a->max_len[axis] <= hs2g::kFewMaxLen;
 }
 bool few_x(const hs2g_adjoint* a) {
-  return a->nxgroups <= hs2g::kFewXGroups && a->max_len[0] <= hs2g::kFewMaxLen;
+  return a->nxgroups <= hs2g::kFewXGroups && a->max_len[0] <= hs2g::kFewMaxNx;
 }
-void ysolve(hs2g_adjoint* a, cudaStream_t st, int axis, const double* rhs, double* y, const double* T_in,
-            double* T_out) {
+template <bool HAS_M, bool ADD_T>
+void launch_ysolve(const hs2g::AView& v, cudaStream_t st, int axis, int64_t nl, const double* M, const double* rhs,
+                   const double* e, const double* u, const double* ip, double* y, const double* T_in,
+                   double* T_out) {
+  hs2g::adj_ysolve_kernel<HAS_M, ADD_T><<<line_blocks(nl), line_threads(nl), 0, st>>>(v, axis, nl, M, rhs, e, u, ip,
+                                                                                       y, T_in, T_out);
+}
+// y = A_a^-1 (M rhs) on the y or z lines (M null: A_a^-1 rhs); T_out = T_in + y when T_out is given
+void ysolve(hs2g_adjoint* a, cudaStream_t st, int axis, const double* M, const double* rhs, double* y,
+            const double* T_in, double* T_out) {
   const hs2g::AView v = view(a);
   const int64_t nl = a->nlines[axis];
+  const double *e = a->e[axis], *u = a->u[axis], *ip = a->ip[axis];
   if (few_lines(a, axis))
     hs2g::adj_ysolve_few_kernel<<<line_blocks(nl), 32, hs2g::few_smem_bytes(a->max_len[axis]), st>>>(
-        v, axis, nl, a->max_len[axis], a->M, rhs, a->lo[axis], a->u[axis], a->ip[axis], y, T_in, T_out);
+        v, axis, nl, a->max_len[axis], M, rhs, e, u, ip, y, T_in, T_out);
+  else if (M && T_out)
+    launch_ysolve<true, true>(v, st, axis, nl, M, rhs, e, u, ip, y, T_in, T_out);
+  else if (M)
+    launch_ysolve<true, false>(v, st, axis, nl, M, rhs, e, u, ip, y, T_in, T_out);
+  else if (T_out)
+    launch_ysolve<false, true>(v, st, axis, nl, M, rhs, e, u, ip, y, T_in, T_out);
   else
-    hs2g::adj_ysolve_kernel<<<line_blocks(nl), line_threads(nl), 0, st>>>(
-        v, axis, nl, a->M, rhs, a->lo[axis], a->u[axis], a->ip[axis], y, T_in, T_out);
-}
-void ysolve_t(hs2g_adjoint* a, cudaStream_t st, int axis, const double* M, const double* rhs, double* mu) {
-  const hs2g::AView v = view(a);
-  const int64_t nl = a->nlines[axis];
-  if (few_lines(a, axis))
-    hs2g::adj_ysolve_t_few_kernel<<<line_blocks(nl), 32, hs2g::few_smem_bytes(a->max_len[axis]), st>>>(
-        v, axis, nl, a->max_len[axis], M, rhs, a->lo[axis], a->u[axis], a->ip[axis], mu);
-  else
-    hs2g::adj_ysolve_t_kernel<<<line_blocks(nl), line_threads(nl), 0, st>>>(
-        v, axis, nl, M, rhs, a->lo[axis], a->u[axis], a->ip[axis], mu);
+    launch_ysolve<false, false>(v, st, axis, nl, M, rhs, e, u, ip, y, T_in, T_out);
 }
 
 // one forward step T_in -> T_out on stream st keeping y0, y1, y2 (T_out may alias T_in; NULL skips it)
@@ -1048,30 +820,32 @@ cudaError_t fwd_step(hs2g_adjoint* a, cudaStream_t st, const double* T_in, doubl
   const hs2g::AView v = view(a);
   if (few_x(a)) {
     hs2g::adj_resid_kernel<<<nblk(a->n), kTh, 0, st>>>(v, T_in, a->g[0], a->g[1], a->g[2], a->D, a->q, s, y0);
-    hs2g::adj_xsolve_few_kernel<<<(unsigned)a->nxgroups, 128, hs2g::few_x_smem_bytes(a->max_len[0]), st>>>(
-        v, a->max_len[0], y0, a->lo[0], a->u[0], a->ip[0], y0);
+    hs2g::adj_xsolve_few_kernel<<<(unsigned)a->nxgroups, 128, hs2g::few_x_smem_bytes(a->max_len[0], 3), st>>>(
+        v, a->max_len[0], nullptr, y0, a->e[0], a->u[0], a->ip[0], y0);
   } else {
-    hs2g::adj_xfwd_kernel<<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(v, T_in, a->g[0], a->g[1], a->g[2], a->D, a->q,
-                                                                        s, a->lo[0], a->u[0], a->ip[0], y0);
+    hs2g::adj_xsolve_kernel<true><<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(
+        v, T_in, a->g[0], a->g[1], a->g[2], a->D, a->q, s, nullptr, nullptr, a->e[0], a->u[0], a->ip[0], y0);
   }
-  ysolve(a, st, 1, y0, y1, nullptr, nullptr);
-  ysolve(a, st, 2, y1, y2, T_in, T_out);
+  ysolve(a, st, 1, a->M, y0, y1, nullptr, nullptr);
+  ysolve(a, st, 2, a->M, y1, y2, T_in, T_out);
   return cudaGetLastError();
 }
 
-// adjoint of one step: lambda (the adjoint of T_{n+1}) -> the adjoint of T_n, gradients accumulated
+// adjoint of one step: lambda (the adjoint of T_{n+1}) -> the adjoint of T_n, gradients accumulated.
+// A_a is symmetric, so the transposed solves A_a^-T are the forward line solves.
 cudaError_t bwd_step(hs2g_adjoint* a, const double* Tn, const double* y0, const double* y1, const double* y2,
                      double s, int64_t obs_step) {
   const hs2g::AView v = view(a);
   cudaStream_t st = a->stream;
-  ysolve_t(a, st, 2, nullptr, a->lam, a->mu[2]);
-  ysolve_t(a, st, 1, a->M, a->mu[2], a->mu[1]);
+  ysolve(a, st, 2, nullptr, a->lam, a->mu[2], nullptr, nullptr);
+  ysolve(a, st, 1, a->M, a->mu[2], a->mu[1], nullptr, nullptr);
   if (few_x(a))
-    hs2g::adj_xsolve_t_few_kernel<<<(unsigned)a->nxgroups, 128, hs2g::few_x_smem_bytes(a->max_len[0]), st>>>(
-        v, a->max_len[0], a->M, a->mu[1], a->lo[0], a->u[0], a->ip[0], a->mu[0]);
+    hs2g::adj_xsolve_few_kernel<<<(unsigned)a->nxgroups, 128, hs2g::few_x_smem_bytes(a->max_len[0], 4), st>>>(
+        v, a->max_len[0], a->M, a->mu[1], a->e[0], a->u[0], a->ip[0], a->mu[0]);
   else
-    hs2g::adj_xsolve_t_kernel<<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(v, a->M, a->mu[1], a->lo[0], a->u[0],
-                                                                            a->ip[0], a->mu[0]);
+    hs2g::adj_xsolve_kernel<false><<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(
+        v, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0.0, a->M, a->mu[1], a->e[0], a->u[0], a->ip[0],
+        a->mu[0]);
   hs2g::adj_update_kernel<<<nblk(a->n), kTh, 0, st>>>(v, a->g[0], a->g[1], a->g[2], Tn, y0, y1, y2, a->mu[0],
                                                       a->mu[1], a->mu[2], s, a->obs, obs_step, a->lam, a->gg[0],
                                                       a->gg[1], a->gg[2], a->gM, a->gq);
@@ -1080,7 +854,7 @@ cudaError_t bwd_step(hs2g_adjoint* a, const double* Tn, const double* y0, const 
 
 void adj_free(hs2g_adjoint* a) {
   void* ptrs[] = {a->inst, a->vox_off, a->line_off, a->xg_off, a->k, a->C, a->q, a->M, a->D, a->g[0], a->g[1],
-                  a->g[2], a->lo[0], a->lo[1], a->lo[2], a->u[0], a->u[1], a->u[2], a->ip[0], a->ip[1], a->ip[2],
+                  a->g[2], a->e[0], a->e[1], a->e[2], a->u[0], a->u[1], a->u[2], a->ip[0], a->ip[1], a->ip[2],
                   a->obs, a->ckpts, a->seg, a->seg2, a->T, a->lam, a->mu[0], a->mu[1], a->mu[2], a->gg[0], a->gg[1],
                   a->gg[2], a->gM, a->gq, a->parts};
   for (void* p : ptrs)
@@ -1170,20 +944,14 @@ int hs2g_adjoint_create(int n, const hs2g_adjoint_grid* grids, double dt, int de
     e = cudaFuncSetAttribute(hs2g::adj_ysolve_few_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)hs2g::few_smem_bytes(hs2g::kFewMaxLen));
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(hs2g::adj_ysolve_t_few_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)hs2g::few_smem_bytes(hs2g::kFewMaxLen));
-  if (e == cudaSuccess)
     e = cudaFuncSetAttribute(hs2g::adj_xsolve_few_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)hs2g::few_x_smem_bytes(hs2g::kFewMaxLen));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(hs2g::adj_xsolve_t_few_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)hs2g::few_x_smem_bytes(hs2g::kFewMaxLen));
+                             (int)hs2g::few_x_smem_bytes(hs2g::kFewMaxNx, 4));
   if (e == cudaSuccess) e = cudaMalloc(&a->inst, sizeof(hs2g::AInst) * n);
   if (e == cudaSuccess) e = cudaMalloc(&a->vox_off, sizeof(int64_t) * (n + 1));
   if (e == cudaSuccess) e = cudaMalloc(&a->line_off, sizeof(int64_t) * 3 * (n + 1));
   if (e == cudaSuccess) e = cudaMalloc(&a->xg_off, sizeof(int64_t) * (n + 1));
-  double** per_voxel[] = {&a->k, &a->C, &a->q, &a->M, &a->D, &a->g[0], &a->g[1], &a->g[2], &a->lo[0], &a->lo[1],
-                          &a->lo[2], &a->u[0], &a->u[1], &a->u[2], &a->ip[0], &a->ip[1], &a->ip[2], &a->T,
+  double** per_voxel[] = {&a->k, &a->C, &a->q, &a->M, &a->D, &a->g[0], &a->g[1], &a->g[2], &a->e[0], &a->e[1],
+                          &a->e[2], &a->u[0], &a->u[1], &a->u[2], &a->ip[0], &a->ip[1], &a->ip[2], &a->T,
                           &a->lam, &a->mu[0], &a->mu[1], &a->mu[2], &a->gg[0], &a->gg[1], &a->gg[2], &a->gM,
                           &a->gq};
   const int nfields = (int)(sizeof(per_voxel) / sizeof(per_voxel[0]));
@@ -1252,7 +1020,7 @@ int hs2g_adjoint_set_parameters(hs2g_adjoint* a, const double* k, const double* 
   hs2g::adj_setup_kernel<<<nblk(n), kTh, 0, st>>>(v, a->k, a->C, 1.0 / a->dt, a->g[0], a->g[1], a->g[2], a->M);
   hs2g::adj_diag_kernel<<<nblk(n), kTh, 0, st>>>(v, a->g[0], a->g[1], a->g[2], a->D);
   for (int ax = 0; ax < 3; ++ax)
-    hs2g::adj_factor_kernel<<<nblk(a->nlines[ax]), kTh, 0, st>>>(v, ax, a->nlines[ax], a->M, a->g[ax], a->lo[ax],
+    hs2g::adj_factor_kernel<<<nblk(a->nlines[ax]), kTh, 0, st>>>(v, ax, a->nlines[ax], a->M, a->g[ax], a->e[ax],
                                                                 a->u[ax], a->ip[ax]);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -1,10 +1,11 @@
 """A numpy model of libhs2g's adjoint kernels (hs2g_adjoint.cu), operation for operation (test helper, CPU).
 
-It repeats the forward step in the LU form the device uses (per-line factors lo, u, 1/pivot), the
-checkpointed forward pass, the segment-by-segment recompute and the reverse sweep -- transposed solves in the
-order z, y, x, then lambda += L mu0, the face / capacity / source gradient accumulation and the chain to k
-and C -- so the adjoint's derivation and its checkpoint bookkeeping can be checked against autograd through
-``torch_adi`` on machines without a GPU.  It is never used by the product.
+It repeats the forward step in the LU form the device uses (per-line factors lo/pivot, u, 1/pivot), the
+checkpointed forward pass, the segment-by-segment recompute and the reverse sweep -- solves with the
+transposed line operators (equal to the forward ones, A being symmetric) in the order z, y, x, then
+lambda += L mu0, the face / capacity / source gradient accumulation and the chain to k and C -- so the
+adjoint's derivation and its checkpoint bookkeeping can be checked against autograd through ``torch_adi`` on
+machines without a GPU.  It is never used by the product.
 """
 import numpy as np
 
@@ -22,11 +23,11 @@ def low_faces(k, spacing):
 
 
 def factor(M, g, axis):
-    """(lo, u, ip) of M - L_axis/2 along `axis`, as adj_factor_kernel."""
+    """(e, u, ip) of M - L_axis/2 along `axis`, as adj_factor_kernel: e = lo / piv, u = super / piv, ip = 1/piv."""
     Mt = np.moveaxis(M, axis, -1)
     gt = np.moveaxis(g, axis, -1)
     n = Mt.shape[-1]
-    lo = np.zeros_like(Mt)
+    e = np.zeros_like(Mt)
     u = np.zeros_like(Mt)
     ip = np.zeros_like(Mt)
     u_prev = np.zeros(Mt.shape[:-1])
@@ -36,47 +37,31 @@ def factor(M, g, axis):
         l = -(0.5 * gl)
         piv = Mt[..., r] + 0.5 * (gl + gh) - u_prev * l
         uu = -(0.5 * gh) / piv
-        lo[..., r] = l
+        inv = 1.0 / piv
+        e[..., r] = l * inv
         u[..., r] = uu
-        ip[..., r] = 1.0 / piv
+        ip[..., r] = inv
         u_prev = uu
-    return tuple(np.moveaxis(a, -1, axis) for a in (lo, u, ip))
+    return tuple(np.moveaxis(a, -1, axis) for a in (e, u, ip))
 
 
 def solve(f, b, axis):
-    lo, u, ip = (np.moveaxis(a, axis, -1) for a in f)
+    """A^-1 b along `axis` in the two one-FMA passes of the device's line solves:
+    z_r = c_r - e_r z_{r-1} with c_r = b_r ip_r (ascending), y_r = z_r - u_r y_{r+1} (descending).
+    A is symmetric, so the adjoint's transposed solves are this solve too."""
+    e, u, ip = (np.moveaxis(a, axis, -1) for a in f)
     bt = np.moveaxis(b, axis, -1)
     n = bt.shape[-1]
     y = np.zeros_like(bt)
     z = np.zeros(bt.shape[:-1])
     for r in range(n):
-        z = (bt[..., r] - lo[..., r] * z) * ip[..., r]
+        z = bt[..., r] * ip[..., r] - e[..., r] * z
         y[..., r] = z
     x = np.zeros(bt.shape[:-1])
     for r in range(n - 1, -1, -1):
         x = y[..., r] - u[..., r] * x
         y[..., r] = x
     return np.moveaxis(y, -1, axis)
-
-
-def solve_t(f, b, axis):
-    lo, u, ip = (np.moveaxis(a, axis, -1) for a in f)
-    bt = np.moveaxis(b, axis, -1)
-    n = bt.shape[-1]
-    mu = np.zeros_like(bt)
-    w = np.zeros(bt.shape[:-1])
-    u_prev = np.zeros(bt.shape[:-1])
-    for r in range(n):
-        w = bt[..., r] - u_prev * w
-        u_prev = u[..., r]
-        mu[..., r] = w
-    x = np.zeros(bt.shape[:-1])
-    lo_next = np.zeros(bt.shape[:-1])
-    for r in range(n - 1, -1, -1):
-        x = (mu[..., r] - lo_next * x) * ip[..., r]
-        lo_next = lo[..., r]
-        mu[..., r] = x
-    return np.moveaxis(mu, -1, axis)
 
 
 def lap(T, gz, gy, gx):
@@ -158,9 +143,9 @@ class Model(object):
                 T = Tn
             for s in range(s1 - 1, s0 - 1, -1):
                 Tn, y0, y1, y2 = slots[s - s0]
-                mu2 = solve_t(self.f[2], lam, 0)
-                mu1 = solve_t(self.f[1], self.M * mu2, 1)
-                mu0 = solve_t(self.f[0], self.M * mu1, 2)
+                mu2 = solve(self.f[2], lam, 0)
+                mu1 = solve(self.f[1], self.M * mu2, 1)
+                mu0 = solve(self.f[0], self.M * mu1, 2)
                 lam = lam + lap(mu0, gz, gy, gx)
                 if s >= 1:
                     lam[0] += 2.0 * (Tn[0] - self.obs[s - 1])
