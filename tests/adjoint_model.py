@@ -77,7 +77,7 @@ def lap(T, gz, gy, gx):
 
 
 def residual(T, q, s, gz, gy, gx, D):
-    """s q - D T + sum over faces of G T_nbr, the forward x stage's residual (adj_xfwd_kernel)."""
+    """s q - D T + sum over faces of G T_nbr, the forward x stage's residual (residual_at in hs2g_adjoint.cu)."""
     r = s * q - D * T
     r[:, :, 1:] += gx[:, :, 1:] * T[:, :, :-1]
     r[:, :, :-1] += gx[:, :, 1:] * T[:, :, 1:]
