@@ -334,16 +334,15 @@ __global__ void __launch_bounds__(128, 4) adj_ysolve_kernel(AView v, int axis, i
 }
 
 // Few-line form of adj_ysolve_kernel.  A small problem (4096 y-lines of 128 rows at 32x128x128) leaves each
-// SM about one warp, whose line is then a chain of memory round trips, one per block of rows.  Here a
-// 32-thread CTA streams its lines' rows through a ring of kFS stages of kFR rows with cp.async (each thread
-// copies its own line's elements, so no barrier is needed), keeping up to (kFS - 1) * kFR rows in flight, and
-// holds the first pass's values of the whole line in shared memory for the second pass.  Same operations,
-// same order, same rounding as adj_ysolve_kernel.
-// What bounds it is the lone warp's own instruction stream (about 6 cycles per instruction with nothing to
-// interleave), not memory: at 32x128x128 the 128-row y solve takes 38 us, 26 us of it with the copies left out
-// (a timing probe); eight ring stages or 16-row stages were slower, and staging each block's operands in
-// registers changed nothing.  Spreading the lines over four 8-lane warps gave the same y time and doubled the
-// z time.
+// SM about one warp, whose line is then a chain of memory round trips, one per block of rows.  Here the rows
+// of a CTA's 32 lines stream through a ring of kFS stages of kFR rows with cp.async, and the first pass's
+// values of the whole line stay in shared memory for the second pass.  Same operations, same order, same
+// rounding as adj_ysolve_kernel.
+// What bounds it is the recurrence warp's own instruction stream (about 6 cycles per instruction with
+// nothing to interleave), not memory: at 32x128x128 the 128-row y solve took 38 us with one warp issuing both
+// the copies and the recurrence, 26 us with the copies left out (a timing probe) and takes 31 us with the
+// copies on a second warp.  Eight ring stages or 16-row stages were slower, staging each block's operands in
+// registers changed nothing, and spreading the lines over four 8-lane warps doubled the z time.
 constexpr int kFS = 4;            // ring stages
 constexpr int kFR = 8;            // rows per stage
 constexpr int kFewMaxLen = 512;   // longest line the few-line kernels hold (128 KB of line values)
@@ -372,76 +371,94 @@ struct FewRing {
   }
 };
 
-__global__ void __launch_bounds__(32) adj_ysolve_few_kernel(AView v, int axis, int64_t nlines, int64_t max_len,
+__device__ __forceinline__ void named_bar_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(nthreads) : "memory");
+}
+__device__ __forceinline__ void named_bar_arrive(int id, int nthreads) {
+  asm volatile("bar.arrive %0, %1;\n" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// Two warps per CTA over the same 32 lines (lane = line): warp 1 issues the copies, warp 0 runs the
+// recurrence.  Ring slot s is handed over with named barriers, FULL(s) = 1 + s from producer to consumer once
+// the slot's copies have landed, EMPTY(s) = 1 + kFS + s back once it is consumed.  Both warps count the blocks
+// of the two passes as one sequence q = 0 .. 2 nb - 1 (nb = blocks of the CTA's longest line), slot q % kFS,
+// and run the same barrier sequence whatever their lines' lengths, so every barrier is met.
+constexpr int kFewLag = 2;  // blocks the producer keeps in flight before handing the oldest over
+
+__global__ void __launch_bounds__(64) adj_ysolve_few_kernel(AView v, int axis, int64_t nlines, int64_t max_len,
                                                             const double* __restrict__ M, const double* rhs,
                                                             const double* __restrict__ e,
                                                             const double* __restrict__ u,
                                                             const double* __restrict__ ip, double* y,
                                                             const double* T_in, double* T_out) {
   extern __shared__ double few_sm[];
-  const int lane = threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t t = blockIdx.x * (int64_t)32 + lane;
-  if (t >= nlines) return;
-  const Line ln = line_at(v, axis, t);
+  const Line ln = t < nlines ? line_at(v, axis, t) : Line{0, 0, 0};
   double* line = few_sm;  // line[r * 32 + lane]
   const FewRing R{few_sm + 32 * max_len, lane};
-  const int len = (int)ln.len, nb = (len + kFR - 1) / kFR;
-  // every issue commits a group (empty past the line's end), so exactly kFS - 1 groups are younger than the
-  // one waited for
-  auto issue_asc = [&](int g) {
-    if (g < nb)
+  const int len = (int)ln.len;
+  const int nb = __reduce_max_sync(0xffffffffu, (len + kFR - 1) / kFR), nq = 2 * nb;
+  if (warp == 1) {
+    // producer: block q < nb is rows [q kFR, q kFR + kFR) ascending (rhs, e, ip, M), block q >= nb rows
+    // len - 1 - (q - nb) kFR - k descending (u, T_in)
+    for (int q = 0; q < nq; ++q) {
+      if (q >= kFS) named_bar_sync(1 + kFS + q % kFS, 64);  // the consumer is done with block q - kFS
       for (int k = 0; k < kFR; ++k) {
-        const int r = g * kFR + k;
-        if (r < len) {
-          const int64_t p = ln.base + r * ln.stride;
-          cp_async8(R.at(g, k, 0), rhs + p);
-          cp_async8(R.at(g, k, 1), e + p);
-          cp_async8(R.at(g, k, 2), ip + p);
-          if (M) cp_async8(R.at(g, k, 3), M + p);
+        if (q < nb) {
+          const int r = q * kFR + k;
+          if (r < len) {
+            const int64_t p = ln.base + r * ln.stride;
+            cp_async8(R.at(q, k, 0), rhs + p);
+            cp_async8(R.at(q, k, 1), e + p);
+            cp_async8(R.at(q, k, 2), ip + p);
+            if (M) cp_async8(R.at(q, k, 3), M + p);
+          }
+        } else {
+          const int r = len - 1 - ((q - nb) * kFR + k);
+          if (r >= 0) {
+            const int64_t p = ln.base + r * ln.stride;
+            cp_async8(R.at(q, k, 0), u + p);
+            if (T_out) cp_async8(R.at(q, k, 1), T_in + p);
+          }
         }
       }
-    cp_async_commit();
-  };
-  for (int g = 0; g < kFS - 1; ++g) issue_asc(g);
-  double z = 0.0;
-  for (int g = 0; g < nb; ++g) {
-    issue_asc(g + kFS - 1);  // into the slot consumed in the previous iteration
-    cp_async_wait<kFS - 1>();
-    for (int k = 0; k < kFR; ++k) {
-      const int r = g * kFR + k;
-      if (r < len) {
-        const double b = M ? __dmul_rn(*R.at(g, k, 3), *R.at(g, k, 0)) : *R.at(g, k, 0);
-        z = __fma_rn(-*R.at(g, k, 1), z, __dmul_rn(b, *R.at(g, k, 2)));
-        line[r * 32 + lane] = z;
+      cp_async_commit();
+      if (q >= kFewLag) {
+        cp_async_wait<kFewLag>();  // block q - kFewLag has landed
+        __threadfence_block();
+        named_bar_arrive(1 + (q - kFewLag) % kFS, 64);
       }
     }
+    cp_async_wait<0>();
+    __threadfence_block();
+    for (int q = nq > kFewLag ? nq - kFewLag : 0; q < nq; ++q) named_bar_arrive(1 + q % kFS, 64);
+    return;
   }
-  auto issue_desc = [&](int g) {
-    if (g < nb)
+  double z = 0.0, x = 0.0;
+  for (int q = 0; q < nq; ++q) {
+    named_bar_sync(1 + q % kFS, 64);
+    if (q < nb) {
       for (int k = 0; k < kFR; ++k) {
-        const int r = len - 1 - (g * kFR + k);
+        const int r = q * kFR + k;
+        if (r < len) {
+          const double b = M ? __dmul_rn(*R.at(q, k, 3), *R.at(q, k, 0)) : *R.at(q, k, 0);
+          z = __fma_rn(-*R.at(q, k, 1), z, __dmul_rn(b, *R.at(q, k, 2)));
+          line[r * 32 + lane] = z;
+        }
+      }
+    } else {
+      for (int k = 0; k < kFR; ++k) {
+        const int r = len - 1 - ((q - nb) * kFR + k);
         if (r >= 0) {
           const int64_t p = ln.base + r * ln.stride;
-          cp_async8(R.at(g, k, 0), u + p);
-          if (T_out) cp_async8(R.at(g, k, 1), T_in + p);
+          x = __fma_rn(-*R.at(q, k, 0), x, line[r * 32 + lane]);
+          y[p] = x;
+          if (T_out) T_out[p] = __dadd_rn(*R.at(q, k, 1), x);
         }
       }
-    cp_async_commit();
-  };
-  for (int g = 0; g < kFS - 1; ++g) issue_desc(g);
-  double x = 0.0;
-  for (int g = 0; g < nb; ++g) {
-    issue_desc(g + kFS - 1);
-    cp_async_wait<kFS - 1>();
-    for (int k = 0; k < kFR; ++k) {
-      const int r = len - 1 - (g * kFR + k);
-      if (r >= 0) {
-        const int64_t p = ln.base + r * ln.stride;
-        x = __fma_rn(-*R.at(g, k, 0), x, line[r * 32 + lane]);
-        y[p] = x;
-        if (T_out) T_out[p] = __dadd_rn(*R.at(g, k, 1), x);
-      }
     }
+    if (q + kFS < nq) named_bar_arrive(1 + kFS + q % kFS, 64);
   }
 }
 
@@ -802,7 +819,7 @@ void ysolve(hs2g_adjoint* a, cudaStream_t st, int axis, const double* M, const d
   const int64_t nl = a->nlines[axis];
   const double *e = a->e[axis], *u = a->u[axis], *ip = a->ip[axis];
   if (few_lines(a, axis))
-    hs2g::adj_ysolve_few_kernel<<<line_blocks(nl), 32, hs2g::few_smem_bytes(a->max_len[axis]), st>>>(
+    hs2g::adj_ysolve_few_kernel<<<line_blocks(nl), 64, hs2g::few_smem_bytes(a->max_len[axis]), st>>>(
         v, axis, nl, a->max_len[axis], M, rhs, e, u, ip, y, T_in, T_out);
   else if (M && T_out)
     launch_ysolve<true, true>(v, st, axis, nl, M, rhs, e, u, ip, y, T_in, T_out);
