@@ -211,7 +211,9 @@ __global__ void __launch_bounds__(kXT) adj_xsolve_kernel(AView v, const double* 
   double carry = 0.0;
   for (int ch = 0; ch < nch; ++ch) {
     const int64_t i = (int64_t)ch * kXC + lane;
-#pragma unroll 2
+    // four lines' loads in flight per warp (64 registers): the 32-instance adjoint batch at 14.3 gradient
+    // evaluations/s against 13.9 with two and 13.8 with eight
+#pragma unroll 4
     for (int ll = 0; ll < kPer; ++ll) {
       const int l = warp * kPer + ll;
       if (l < g.nl && i < g.nx) {
