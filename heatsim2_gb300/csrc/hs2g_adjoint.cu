@@ -84,14 +84,16 @@ struct Vox {
   int64_t i, j, k, nx, ny, nz, nxy;
   int inst;
 };
+// voxel p -> instance and (k, j, i); 32-bit divisions (hs2g_adjoint_create refuses batches of 2^31 voxels)
 __device__ __forceinline__ Vox vox_at(const AView& v, int64_t p) {
   const int n = find_inst(v.vox_off, v.ninst, p);
   const AInst& in = v.inst[n];
-  const int64_t l = p - in.off;
+  const uint32_t l = (uint32_t)(p - in.off), nx = (uint32_t)in.nx, ny = (uint32_t)in.ny;
+  const uint32_t row = l / nx, k = row / ny;
   Vox r;
   r.inst = n;
   r.nx = in.nx; r.ny = in.ny; r.nz = in.nz; r.nxy = in.nx * in.ny;
-  r.i = l % in.nx; r.j = (l / in.nx) % in.ny; r.k = l / r.nxy;
+  r.i = l - row * nx; r.j = row - k * ny; r.k = k;
   return r;
 }
 
