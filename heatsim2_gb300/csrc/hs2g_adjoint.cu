@@ -400,6 +400,7 @@ __device__ __forceinline__ void named_bar_arrive(int id, int nthreads) {
 // and run the same barrier sequence whatever their lines' lengths, so every barrier is met.
 constexpr int kFewLag = 2;  // blocks the producer keeps in flight before handing the oldest over
 
+template <bool HAS_M, bool ADD_T>
 __global__ void __launch_bounds__(64) adj_ysolve_few_kernel(AView v, int axis, int64_t nlines, int64_t max_len,
                                                             const double* __restrict__ M, const double* rhs,
                                                             const double* __restrict__ e,
@@ -419,6 +420,7 @@ __global__ void __launch_bounds__(64) adj_ysolve_few_kernel(AView v, int axis, i
     // len - 1 - (q - nb) kFR - k descending (u, T_in)
     for (int q = 0; q < nq; ++q) {
       if (q >= kFS) named_bar_sync(1 + kFS + q % kFS, 64);  // the consumer is done with block q - kFS
+#pragma unroll
       for (int k = 0; k < kFR; ++k) {
         if (q < nb) {
           const int r = q * kFR + k;
@@ -427,14 +429,14 @@ __global__ void __launch_bounds__(64) adj_ysolve_few_kernel(AView v, int axis, i
             cp_async8(R.at(q, k, 0), rhs + p);
             cp_async8(R.at(q, k, 1), e + p);
             cp_async8(R.at(q, k, 2), ip + p);
-            if (M) cp_async8(R.at(q, k, 3), M + p);
+            if (HAS_M) cp_async8(R.at(q, k, 3), M + p);
           }
         } else {
           const int r = len - 1 - ((q - nb) * kFR + k);
           if (r >= 0) {
             const int64_t p = ln.base + r * ln.stride;
             cp_async8(R.at(q, k, 0), u + p);
-            if (T_out) cp_async8(R.at(q, k, 1), T_in + p);
+            if (ADD_T) cp_async8(R.at(q, k, 1), T_in + p);
           }
         }
       }
@@ -454,22 +456,24 @@ __global__ void __launch_bounds__(64) adj_ysolve_few_kernel(AView v, int axis, i
   for (int q = 0; q < nq; ++q) {
     named_bar_sync(1 + q % kFS, 64);
     if (q < nb) {
+#pragma unroll
       for (int k = 0; k < kFR; ++k) {
         const int r = q * kFR + k;
         if (r < len) {
-          const double b = M ? __dmul_rn(*R.at(q, k, 3), *R.at(q, k, 0)) : *R.at(q, k, 0);
+          const double b = HAS_M ? __dmul_rn(*R.at(q, k, 3), *R.at(q, k, 0)) : *R.at(q, k, 0);
           z = __fma_rn(-*R.at(q, k, 1), z, __dmul_rn(b, *R.at(q, k, 2)));
           line[r * 32 + lane] = z;
         }
       }
     } else {
+#pragma unroll
       for (int k = 0; k < kFR; ++k) {
         const int r = len - 1 - ((q - nb) * kFR + k);
         if (r >= 0) {
           const int64_t p = ln.base + r * ln.stride;
           x = __fma_rn(-*R.at(q, k, 0), x, line[r * 32 + lane]);
           y[p] = x;
-          if (T_out) T_out[p] = __dadd_rn(*R.at(q, k, 1), x);
+          if (ADD_T) T_out[p] = __dadd_rn(*R.at(q, k, 1), x);
         }
       }
     }
@@ -534,7 +538,8 @@ __device__ __forceinline__ void few_x_issue(const FewX& F, const XGroup& g, int 
   cp_async_commit();
 }
 
-// y = A_x^-1 (M rhs), or A_x^-1 rhs when M is null (rhs = r0 in the forward stage; rhs may alias y)
+// y = A_x^-1 (M rhs) (HAS_M), or A_x^-1 rhs (rhs = r0 in the forward stage; rhs may alias y)
+template <bool HAS_M>
 __global__ void __launch_bounds__(128) adj_xsolve_few_kernel(AView v, int64_t max_nx, const double* __restrict__ M,
                                                              const double* rhs, const double* __restrict__ e,
                                                              const double* __restrict__ u,
@@ -544,25 +549,32 @@ __global__ void __launch_bounds__(128) adj_xsolve_few_kernel(AView v, int64_t ma
   // warp w solves the group's lines [lb, le): it copies them with lane = column and recurs with lane = line
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int lb = min(warp * kFewLanes, (int)g.nl), le = min(lb + kFewLanes, (int)g.nl), ln = lb + lane;
-  const FewX F{few_sm, few_sm + kXL * (max_nx + 1), max_nx + 1, M ? 4 : 3};
+  const FewX F{few_sm, few_sm + kXL * (max_nx + 1), max_nx + 1, HAS_M ? 4 : 3};
+  const double* Mop = HAS_M ? M : nullptr;
   const int nch = (int)((g.nx + kXC - 1) / kXC);
-  for (int q = 0; q < kXFS - 1; ++q) few_x_issue(F, g, q, q < nch ? q : -1, lane, lb, le, rhs, e, ip, M);
+  for (int q = 0; q < kXFS - 1; ++q) few_x_issue(F, g, q, q < nch ? q : -1, lane, lb, le, rhs, e, ip, Mop);
   double z = 0.0;
   for (int ch = 0; ch < nch; ++ch) {
     __syncwarp();  // every lane is done with the slot refilled here
     const int nxt = ch + kXFS - 1;
-    few_x_issue(F, g, nxt, nxt < nch ? nxt : -1, lane, lb, le, rhs, e, ip, M);
+    few_x_issue(F, g, nxt, nxt < nch ? nxt : -1, lane, lb, le, rhs, e, ip, Mop);
     cp_async_wait<kXFS - 1>();
     __syncwarp();  // chunk ch's copies by every lane are visible
     if (ln < le) {
       const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
       const double *tb = F.tile(ch, 0, ln), *te = F.tile(ch, 1, ln), *ti = F.tile(ch, 2, ln);
-      const double* tm = M ? F.tile(ch, 3, ln) : tb;
+      const double* tm = HAS_M ? F.tile(ch, 3, ln) : tb;
       double* zr = F.lines + ln * F.zs + ch * kXC;
-      for (int cc = 0; cc < cw; ++cc) {
-        const double b = M ? __dmul_rn(tm[cc], tb[cc]) : tb[cc];
+      auto step = [&](int cc) {
+        const double b = HAS_M ? __dmul_rn(tm[cc], tb[cc]) : tb[cc];
         z = __fma_rn(-te[cc], z, __dmul_rn(b, ti[cc]));
         zr[cc] = z;
+      };
+      if (cw == kXC) {
+#pragma unroll 8
+        for (int cc = 0; cc < kXC; ++cc) step(cc);
+      } else {
+        for (int cc = 0; cc < cw; ++cc) step(cc);
       }
     }
   }
@@ -580,9 +592,15 @@ __global__ void __launch_bounds__(128) adj_xsolve_few_kernel(AView v, int64_t ma
       const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
       const double* tu = F.tile(q, 0, ln);
       double* zr = F.lines + ln * F.zs + ch * kXC;
-      for (int cc = cw - 1; cc >= 0; --cc) {
+      auto step = [&](int cc) {
         x = __fma_rn(-tu[cc], x, zr[cc]);
         zr[cc] = x;
+      };
+      if (cw == kXC) {
+#pragma unroll 8
+        for (int cc = kXC - 1; cc >= 0; --cc) step(cc);
+      } else {
+        for (int cc = cw - 1; cc >= 0; --cc) step(cc);
       }
     }
   }
@@ -833,10 +851,20 @@ void ysolve(hs2g_adjoint* a, cudaStream_t st, int axis, const double* M, const d
   const hs2g::AView v = view(a);
   const int64_t nl = a->nlines[axis];
   const double *e = a->e[axis], *u = a->u[axis], *ip = a->ip[axis];
-  if (few_lines(a, axis))
-    hs2g::adj_ysolve_few_kernel<<<line_blocks(nl), 64, hs2g::few_smem_bytes(a->max_len[axis]), st>>>(
-        v, axis, nl, a->max_len[axis], M, rhs, e, u, ip, y, T_in, T_out);
-  else if (M && T_out)
+  if (few_lines(a, axis)) {
+    const unsigned nbk = line_blocks(nl);
+    const size_t sm = hs2g::few_smem_bytes(a->max_len[axis]);
+    const int64_t ml = a->max_len[axis];
+    if (M && T_out)
+      hs2g::adj_ysolve_few_kernel<true, true><<<nbk, 64, sm, st>>>(v, axis, nl, ml, M, rhs, e, u, ip, y, T_in, T_out);
+    else if (M)
+      hs2g::adj_ysolve_few_kernel<true, false><<<nbk, 64, sm, st>>>(v, axis, nl, ml, M, rhs, e, u, ip, y, T_in, T_out);
+    else if (T_out)
+      hs2g::adj_ysolve_few_kernel<false, true><<<nbk, 64, sm, st>>>(v, axis, nl, ml, M, rhs, e, u, ip, y, T_in, T_out);
+    else
+      hs2g::adj_ysolve_few_kernel<false, false><<<nbk, 64, sm, st>>>(v, axis, nl, ml, M, rhs, e, u, ip, y, T_in,
+                                                                      T_out);
+  } else if (M && T_out)
     launch_ysolve<true, true>(v, st, axis, nl, M, rhs, e, u, ip, y, T_in, T_out);
   else if (M)
     launch_ysolve<true, false>(v, st, axis, nl, M, rhs, e, u, ip, y, T_in, T_out);
@@ -852,7 +880,7 @@ cudaError_t fwd_step(hs2g_adjoint* a, cudaStream_t st, const double* T_in, doubl
   const hs2g::AView v = view(a);
   if (few_x(a)) {
     hs2g::adj_resid_kernel<<<nblk(a->n), kTh, 0, st>>>(v, T_in, a->g[0], a->g[1], a->g[2], a->D, a->q, s, y0);
-    hs2g::adj_xsolve_few_kernel<<<(unsigned)a->nxgroups, 128, hs2g::few_x_smem_bytes(a->max_len[0], 3), st>>>(
+    hs2g::adj_xsolve_few_kernel<false><<<(unsigned)a->nxgroups, 128, hs2g::few_x_smem_bytes(a->max_len[0], 3), st>>>(
         v, a->max_len[0], nullptr, y0, a->e[0], a->u[0], a->ip[0], y0);
   } else {
     hs2g::adj_xsolve_kernel<true><<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(
@@ -872,7 +900,7 @@ cudaError_t bwd_step(hs2g_adjoint* a, const double* Tn, const double* y0, const 
   ysolve(a, st, 2, nullptr, a->lam, a->mu[2], nullptr, nullptr);
   ysolve(a, st, 1, a->M, a->mu[2], a->mu[1], nullptr, nullptr);
   if (few_x(a))
-    hs2g::adj_xsolve_few_kernel<<<(unsigned)a->nxgroups, 128, hs2g::few_x_smem_bytes(a->max_len[0], 4), st>>>(
+    hs2g::adj_xsolve_few_kernel<true><<<(unsigned)a->nxgroups, 128, hs2g::few_x_smem_bytes(a->max_len[0], 4), st>>>(
         v, a->max_len[0], a->M, a->mu[1], a->e[0], a->u[0], a->ip[0], a->mu[0]);
   else
     hs2g::adj_xsolve_kernel<false><<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(
@@ -974,12 +1002,22 @@ int hs2g_adjoint_create(int n, const hs2g_adjoint_grid* grids, double dt, int de
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&a->ev_done[b], cudaEventDisableTiming);
   }
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&a->ev_start, cudaEventDisableTiming);
+  {
+    const void* few_y[] = {(const void*)hs2g::adj_ysolve_few_kernel<true, true>,
+                           (const void*)hs2g::adj_ysolve_few_kernel<true, false>,
+                           (const void*)hs2g::adj_ysolve_few_kernel<false, true>,
+                           (const void*)hs2g::adj_ysolve_few_kernel<false, false>};
+    for (const void* f : few_y)
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)hs2g::few_smem_bytes(hs2g::kFewMaxLen));
+  }
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(hs2g::adj_ysolve_few_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)hs2g::few_smem_bytes(hs2g::kFewMaxLen));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(hs2g::adj_xsolve_few_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(hs2g::adj_xsolve_few_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)hs2g::few_x_smem_bytes(hs2g::kFewMaxNx, 4));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(hs2g::adj_xsolve_few_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)hs2g::few_x_smem_bytes(hs2g::kFewMaxNx, 3));
   if (e == cudaSuccess) e = cudaMalloc(&a->inst, sizeof(hs2g::AInst) * n);
   if (e == cudaSuccess) e = cudaMalloc(&a->vox_off, sizeof(int64_t) * (n + 1));
   if (e == cudaSuccess) e = cudaMalloc(&a->line_off, sizeof(int64_t) * 3 * (n + 1));
