@@ -31,7 +31,8 @@ EXPORTED = ("hs2g_abi_version", "hs2g_last_error", "hs2g_create_classes", "hs2g_
             "hs2g_batch_set_clock", "hs2g_batch_run", "hs2g_batch_autotune",
             "hs2g_adjoint_create", "hs2g_adjoint_destroy", "hs2g_adjoint_set_stream", "hs2g_adjoint_layout",
             "hs2g_adjoint_device_bytes", "hs2g_adjoint_set_parameters", "hs2g_adjoint_forward",
-            "hs2g_adjoint_backward", "hs2g_create_rows", "hs2g_selftest_wait")
+            "hs2g_adjoint_backward", "hs2g_create_rows", "hs2g_selftest_wait", "hs2g_run_surface",
+            "hs2g_surface_temperature")
 STATIC_MAX_VOXELS = 1 << 20
 
 
@@ -123,6 +124,10 @@ def load():
         L.hs2g_step.restype = i32
         L.hs2g_run.argtypes = [vp, i32, vp, vp, vp, i32, vp, i32]
         L.hs2g_run.restype = i32
+        L.hs2g_run_surface.argtypes = [vp, i32, vp, vp, vp, dp, vp, i32]
+        L.hs2g_run_surface.restype = i32
+        L.hs2g_surface_temperature.argtypes = [i32, i64, i64, i64, vp, dp, vp, vp, i32]
+        L.hs2g_surface_temperature.restype = i32
         L.hs2g_source_table.argtypes = [i32, vp, vp, dp, dp, dp, vp]
         L.hs2g_source_table.restype = i32
         L.hs2g_get_faces.argtypes = [vp, vp, vp, vp, vp, vp]

@@ -236,30 +236,38 @@ def run_adi_steps(ADI_params, ADI_steps, t, dt, Tarray, volumetric_elements, vol
     return out
 
 
-def run(ADI_params, Tarray, times, dt, volumetric_elements, volumetric, record_layer=None):
+def run(ADI_params, Tarray, times, dt, volumetric_elements, volumetric, record_layer=None, record_surface=False):
     """Advance ``Tarray`` through one step per value in ``times`` (the t passed to each step), on the device.
 
     Equivalent to calling run_adi_steps once per t, but steps without per-voxel sources are queued in one
-    native call.  Returns ``T`` (or ``(T, history)`` with ``record_layer``: the layer z=record_layer after every
-    step, shape (len(times), ny, nx))."""
+    native call.  Returns ``T``, or ``(T, history)`` of shape (len(times), ny, nx) recorded after every step:
+    the layer z=record_layer with ``record_layer``, or with ``record_surface=True`` the z = 0 surface
+    temperature as the reference's ``insulating_z_min_surface_temperature(T, dz)`` estimates it
+    (heatsim2_gb300.surface_temperature)."""
     P = ADI_params
     L = _native.load()
     sources = _ClassSources(volumetric, np.ndim(P.volume_array) > 0)
     nz, ny, nx = P.shape
+    if record_surface and record_layer is not None:
+        raise ValueError("record_layer and record_surface are exclusive")
+    if record_surface and nz < 2:
+        raise ValueError("the surface estimate needs nz >= 2")
+    recording = record_layer is not None or bool(record_surface)
+    dz = float(P.spacing[0])
     times = [float(t) for t in times]
     n = len(times)
     on_dev = _is_torch_cuda(Tarray)
     if on_dev:
         import torch
         T = Tarray.contiguous().clone()
-        hist = torch.empty((n, ny, nx), dtype=torch.float64, device=T.device) if record_layer is not None else None
+        hist = torch.empty((n, ny, nx), dtype=torch.float64, device=T.device) if recording else None
         stream = torch.cuda.current_stream(T.device)
         _native.check(L.hs2g_set_stream(P.handle.ptr, ctypes.c_void_p(stream.cuda_stream)))
         ptr = T.data_ptr()
         flags = _native.DEVICE
     else:
         T = np.ascontiguousarray(Tarray, dtype="d").copy()
-        hist = np.empty((n, ny, nx)) if record_layer is not None else None
+        hist = np.empty((n, ny, nx)) if recording else None
         _native.check(L.hs2g_set_stream(P.handle.ptr, None))
         ptr = T.ctypes.data
         flags = 0
@@ -290,7 +298,11 @@ def run(ADI_params, Tarray, times, dt, volumetric_elements, volumetric, record_l
                                       newmap.ctypes.data if (first and newmap is not None) else None,
                                       flags | _native.SYNC))
             if hist is not None:
-                hist[s] = T[record_layer]
+                if record_surface:
+                    from .surface_temperature import insulating_z_min_surface_temperature
+                    hist[s] = insulating_z_min_surface_temperature(T, dz)
+                else:
+                    hist[s] = T[record_layer]
             s += 1
             first = False
             continue
@@ -299,14 +311,14 @@ def run(ADI_params, Tarray, times, dt, volumetric_elements, volumetric, record_l
             e += 1
         chunk = np.ascontiguousarray(qtabs[s:e])
         if hist is not None:
-            hptr = hist[s:e].data_ptr() if on_dev else np.ascontiguousarray(hist[s:e]).ctypes.data
-            if on_dev:
+            hbuf = hist[s:e] if on_dev else np.empty((e - s, ny, nx))
+            hptr = hbuf.data_ptr() if on_dev else hbuf.ctypes.data
+            if record_surface:
+                _native.check(L.hs2g_run_surface(P.handle.ptr, e - s, ptr, ptr, chunk.ctypes.data, dz, hptr, flags))
+            else:
                 _native.check(L.hs2g_run(P.handle.ptr, e - s, ptr, ptr, chunk.ctypes.data, int(record_layer), hptr,
                                          flags))
-            else:
-                hbuf = np.empty((e - s, ny, nx))
-                _native.check(L.hs2g_run(P.handle.ptr, e - s, ptr, ptr, chunk.ctypes.data, int(record_layer),
-                                         hbuf.ctypes.data, flags))
+            if not on_dev:
                 hist[s:e] = hbuf
         else:
             _native.check(L.hs2g_run(P.handle.ptr, e - s, ptr, ptr, chunk.ctypes.data, 0, None, flags))
@@ -314,4 +326,4 @@ def run(ADI_params, Tarray, times, dt, volumetric_elements, volumetric, record_l
         first = False
     if on_dev:
         stream.synchronize()
-    return (T, hist) if record_layer is not None else T
+    return (T, hist) if recording else T

@@ -691,11 +691,11 @@ int hs2g_step(hs2g_handle* h, const double* T_in, double* T_out, const double* q
   return HS2G_OK;
 }
 
-int hs2g_run(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, const double* qtabs,
-             int record_layer, double* history, int flags) {
-  if (!h || !T_in || !T_out || nsteps < 0) return fail(HS2G_ERR_ARG, "bad argument");
-  if (history && (record_layer < 0 || record_layer >= h->d.nz))
-    return fail(HS2G_ERR_ARG, "record_layer %d outside 0..%lld", record_layer, (long long)h->d.nz - 1);
+namespace {
+// hs2g_run and hs2g_run_surface: after every step, history receives layer record_layer of T, or (surface_dz > 0)
+// the insulating z = 0 surface temperature estimated from layers 0 and 1
+int run_steps(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, const double* qtabs, int record_layer,
+              double surface_dz, double* history, int flags) {
   DeviceGuard g(h->device);
   if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", h->device);
   const Dims& d = h->d;
@@ -743,7 +743,9 @@ int hs2g_run(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, cons
     cudaError_t e = hs2g::launch_step(a, h->c, q, s);
     if (e != cudaSuccess) return cuda_fail(e, "step kernels");
     if (hist) {
-      e = hs2g::launch_copy_layer(d, dst, record_layer, hist + (int64_t)st * d.nxy(), s);
+      double* row = hist + (int64_t)st * d.nxy();
+      e = surface_dz > 0.0 ? hs2g::launch_surface_estimate(d.nxy(), dst, surface_dz, row, s)
+                           : hs2g::launch_copy_layer(d, dst, record_layer, row, s);
       if (e != cudaSuccess) return cuda_fail(e, "history copy");
     }
     src = dst;
@@ -762,6 +764,54 @@ int hs2g_run(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, cons
     HS2G_CUDA(cudaStreamSynchronize(s), "run");
     return check_status(h);
   }
+  return HS2G_OK;
+}
+}  // namespace
+
+int hs2g_run(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, const double* qtabs,
+             int record_layer, double* history, int flags) {
+  if (!h || !T_in || !T_out || nsteps < 0) return fail(HS2G_ERR_ARG, "bad argument");
+  if (history && (record_layer < 0 || record_layer >= h->d.nz))
+    return fail(HS2G_ERR_ARG, "record_layer %d outside 0..%lld", record_layer, (long long)h->d.nz - 1);
+  return run_steps(h, nsteps, T_in, T_out, qtabs, record_layer, 0.0, history, flags);
+}
+
+int hs2g_run_surface(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, const double* qtabs, double dz,
+                     double* history, int flags) {
+  if (!h || !T_in || !T_out || !history || nsteps < 0) return fail(HS2G_ERR_ARG, "bad argument");
+  if (!(dz > 0.0) || !std::isfinite(dz)) return fail(HS2G_ERR_ARG, "dz must be positive and finite");
+  if (h->d.nz < 2) return fail(HS2G_ERR_ARG, "the surface estimate needs nz >= 2");
+  return run_steps(h, nsteps, T_in, T_out, qtabs, 0, dz, history, flags);
+}
+
+int hs2g_surface_temperature(int device, int64_t nz, int64_t ny, int64_t nx, const double* T, double dz,
+                             double* out, void* stream, int flags) {
+  if (!T || !out || nz < 2 || ny < 1 || nx < 1 || ny > (int64_t(1) << 40) / nx)
+    return fail(HS2G_ERR_ARG, "bad argument (the surface estimate needs nz >= 2)");
+  if (!(dz > 0.0) || !std::isfinite(dz)) return fail(HS2G_ERR_ARG, "dz must be positive and finite");
+  DeviceGuard g(device);
+  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", device);
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t nxy = ny * nx;
+  if (flags & HS2G_DEVICE) {
+    HS2G_CUDA(hs2g::launch_surface_estimate(nxy, T, dz, out, s), "surface estimate");
+    if (flags & HS2G_SYNC) HS2G_CUDA(cudaStreamSynchronize(s), "surface estimate");
+    return HS2G_OK;
+  }
+  // host pointers: layers 0 and 1 up, the estimate down (temporary device buffers)
+  double* buf = nullptr;
+  cudaError_t e = cudaMalloc(&buf, sizeof(double) * 3 * nxy);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(e == cudaErrorMemoryAllocation ? HS2G_ERR_NOMEM : HS2G_ERR_CUDA, "surface estimate: %s",
+                cudaGetErrorString(e));
+  }
+  e = cudaMemcpyAsync(buf, T, sizeof(double) * 2 * nxy, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = hs2g::launch_surface_estimate(nxy, buf, dz, buf + 2 * nxy, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, buf + 2 * nxy, sizeof(double) * nxy, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(buf);
+  if (e != cudaSuccess) return fail(HS2G_ERR_CUDA, "surface estimate: %s", cudaGetErrorString(e));
   return HS2G_OK;
 }
 

@@ -98,6 +98,8 @@ cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable&
                                cudaEvent_t ev[4]);
 cudaError_t fp64_fma_rate(double* fma_per_s);
 cudaError_t launch_copy_layer(const Dims& d, const double* T, int layer, double* dst, cudaStream_t s);
+// insulating z = 0 surface temperature from layers 0 and 1 of T (an nxy-element plane each) into dst[nxy]
+cudaError_t launch_surface_estimate(int64_t nxy, const double* T, double dz, double* dst, cudaStream_t s);
 // one bounded mbarrier wait on a barrier that receives its arrival (arrive != 0) or none (hs2g_lines.cu)
 cudaError_t wait_selftest(uint64_t limit_ns, int arrive, int* status_dev, cudaStream_t s);
 // the step in pieces, for overlapping host copies with it: the x sweep over x-lines [line_begin, line_end)

@@ -16,6 +16,8 @@
 //   y sweep: TMA tensor tiles (hs2g_lines.cu), or one thread per y-line with plain loads.
 //   z sweep: one thread per z-line (j,i); neighbouring lanes have neighbouring i, so each k step is one
 //            coalesced 256-byte access per array per warp (a TMA variant exists, HS2G_Z_SWEEP=tma).
+#include <cmath>
+
 #include "hs2g_internal.cuh"
 
 namespace hs2g {
@@ -223,6 +225,21 @@ __global__ void copy_layer_kernel(Dims d, const double* __restrict__ T, int laye
   if (t < d.nxy()) dst[t] = T[(int64_t)layer * d.nxy() + t];
 }
 
+// Temperature of the z = 0 surface estimated from layers 0 and 1 as the reference's
+// insulating_z_min_surface_temperature(T, dz) does (surface_temperature.py:4-36): the mean of a quadratic with
+// zero slope at the surface through the two layer centres, c = T0 - (0.25 a) dz^2 with a = (T1 - T0)/(2 dz^2),
+// and the linear extrapolation T0 - (T1 - T0)/2.  Same operations in the same order, each rounding explicit.
+__global__ void surface_estimate_kernel(int64_t nxy, const double* __restrict__ T, double dz2,
+                                        double* __restrict__ dst) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nxy) return;
+  const double t0 = T[t], t1 = T[nxy + t];
+  const double a = __ddiv_rn(__dsub_rn(t1, t0), __dmul_rn(2.0, dz2));
+  const double c = __dsub_rn(t0, __dmul_rn(__dmul_rn(0.25, a), dz2));
+  const double lin = __dsub_rn(t0, __ddiv_rn(__dsub_rn(t1, t0), 2.0));
+  dst[t] = __ddiv_rn(__dadd_rn(lin, c), 2.0);
+}
+
 inline unsigned blocks(int64_t n, int per) { return (unsigned)((n + per - 1) / per); }
 
 // FP64 issue-rate probe: 8 independent FMA chains per thread, registers only, one store per thread.
@@ -335,6 +352,15 @@ cudaError_t launch_z_range(const StepArgs& a, const Coeffs& c, int64_t col_begin
 
 cudaError_t launch_copy_layer(const Dims& d, const double* T, int layer, double* dst, cudaStream_t s) {
   copy_layer_kernel<<<blocks(d.nxy(), 256), 256, 0, s>>>(d, T, layer, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_surface_estimate(int64_t nxy, const double* T, double dz, double* dst, cudaStream_t s) {
+  // dz^2 as the reference's dz**2.0 computes it: the C library's pow, which can differ from dz*dz by an ulp (the
+  // volatile exponent keeps the compiler from replacing the call by a multiplication)
+  volatile double two = 2.0;
+  const double dz2 = std::pow(dz, (double)two);
+  surface_estimate_kernel<<<blocks(nxy, 256), 256, 0, s>>>(nxy, T, dz2, dst);
   return cudaGetLastError();
 }
 

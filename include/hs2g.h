@@ -168,6 +168,24 @@ int hs2g_run(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, cons
              int record_layer, double* history, int flags);
 
 /*
+ * hs2g_run recording, after every step, the temperature of the z = 0 surface as the reference's
+ * insulating_z_min_surface_temperature(T, dz) estimates it from layers 0 and 1 (heatsim2/surface_temperature.py:4-36;
+ * the reference evaluates it in numpy on each step's returned T): history[nsteps][ny][nx].  Needs nz >= 2 and
+ * dz > 0 (m, the layers' thickness).
+ */
+int hs2g_run_surface(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, const double* qtabs, double dz,
+                     double* history, int flags);
+
+/*
+ * The same surface estimate of one (nz, ny, nx) temperature field, no handle needed: out[ny][nx] from T's layers
+ * 0 and 1 on `device`, on `stream` (NULL: the default stream).  With HS2G_DEVICE T and out are device pointers
+ * and the call returns after queuing (unless HS2G_SYNC); otherwise host pointers, copied through temporary
+ * device buffers, and the call synchronises.
+ */
+int hs2g_surface_temperature(int device, int64_t nz, int64_t ny, int64_t nx, const double* T, double dz,
+                             double* out, void* stream, int flags);
+
+/*
  * hs2g_run without history, timing each sweep kernel with CUDA events on the handle's stream.
  * kernel_ms[0..2] receive the summed device time of the x, y and z sweeps over the nsteps steps and
  * kernel_ms[3] the device time from the first event to the last.  Takes device pointers (HS2G_DEVICE).

@@ -201,3 +201,15 @@ def run_adi_steps(params, steps, t, dt, Tarray, volumetric_elements, volumetric)
     if rc != 0:
         raise RuntimeError("oracle step failed")
     return out
+
+
+def insulating_z_min_surface_temperature(T, dz):
+    """heatsim2/surface_temperature.py:4-36: the z = 0 surface temperature from layers 0 and 1 of T[z, y, x],
+    the mean of the zero-slope quadratic through the layer centres (a, c) and the linear extrapolation, with the
+    reference's operations in its order."""
+    T = np.asarray(T, dtype="d")
+    a = (T[1] - T[0]) / (2.0 * dz ** 2.0)
+    c = T[0] - 0.25 * a * dz ** 2.0
+    d = T[1] - T[0]
+    linear = T[0] - d / 2.0
+    return (linear + c) / 2.0

@@ -3,7 +3,7 @@
 Run in a container where the reference sources are mounted (the reference is built into oracle/_ref by
 oracle/build_ref.py first):
 
-    python oracle/build_ref.py && python tests/golden/make_golden.py [curved]
+    python oracle/build_ref.py && python tests/golden/make_golden.py [curved | surface]
 
 Each fixture ``<name>.npz`` holds the problem spec (heatsim2_gb300.workloads serialisation), the t values
 passed to the reference's run_adi_steps, and the temperature field the reference returned after selected
@@ -91,12 +91,33 @@ def curved_fixtures(hs):
     save_fixture("curved_steel_slab", W.curved(W.steel_slab(nsteps=20), seed=22, amplitude=8.0), {1, 5, 20}, hs)
 
 
+def surface_fixture(hs):
+    """The reference's surface-temperature estimate (heatsim2/surface_temperature.py:4-36) of seeded random
+    fields and of the reference's own steel-slab states, for several layer thicknesses."""
+    import heatsim2.surface_temperature as ref_surface
+    rng = np.random.default_rng(31)
+    d = {}
+    fields = [293.0 + rng.random((2, 7, 9)), 293.0 + 50.0 * rng.random((5, 16, 12)),
+              rng.standard_normal((3, 1, 4)) * 1e3]
+    _, _, _, states = run_reference(hs, W.steel_slab(nsteps=12), {1, 12})
+    fields += [np.ascontiguousarray(states["T_1"][:3]), np.ascontiguousarray(states["T_12"][:3])]
+    dzs = [1e-3, 5e-4, 3.7e-3, 1e-3, 1e-3]
+    for c, (F, dz) in enumerate(zip(fields, dzs)):
+        d["T_%d" % c], d["dz_%d" % c] = F, np.float64(dz)
+        d["surface_%d" % c] = ref_surface.insulating_z_min_surface_temperature(F, dz)
+    np.savez_compressed(os.path.join(HERE, "surface_temperature.npz"), **d)
+    print("wrote surface_temperature")
+
+
 def main():
     if not build_ref.available():
         build_ref.build()
     hs = build_ref.import_reference()
     if len(sys.argv) > 1 and sys.argv[1] == "curved":
         curved_fixtures(hs)
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "surface":
+        surface_fixture(hs)
         return
     import heatsim2.tridiag as ref_tridiag
     tridiag_fixture(ref_tridiag)
@@ -111,6 +132,7 @@ def main():
     for shape in ((1, 1, 7), (7, 1, 1), (1, 7, 1), (1, 1, 1), (1, 5, 6), (4, 1, 5), (3, 4, 1)):
         save_fixture("line_%dx%dx%d" % shape, W.line_grid(shape), set(range(1, 6)), hs)
     curved_fixtures(hs)
+    surface_fixture(hs)
 
 
 if __name__ == "__main__":
