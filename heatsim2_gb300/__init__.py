@@ -29,6 +29,7 @@ from . import boundary_thininsulatinglayer  # noqa: F401
 from . import expression  # noqa: F401
 from . import crank_nicolson  # noqa: F401
 from . import alternatingdirection  # noqa: F401
+from . import surface_temperature  # noqa: F401
 from .crank_nicolson import setup, UnalignedAnisotropyError  # noqa: F401
 from .alternatingdirection import run_adi_steps, run  # noqa: F401
 
@@ -109,7 +110,8 @@ def install_as_heatsim2():
     me = sys.modules[__name__]
     sys.modules["heatsim2"] = me
     for sub in ("expression", "crank_nicolson", "alternatingdirection", "boundary_conducting",
-                "boundary_conducting_anisotropic", "boundary_insulating", "boundary_thininsulatinglayer"):
+                "boundary_conducting_anisotropic", "boundary_insulating", "boundary_thininsulatinglayer",
+                "surface_temperature"):
         sys.modules["heatsim2." + sub] = sys.modules[__name__ + "." + sub]
     sys.modules["heatsim2.alternatingdirection_c_pyx"] = sys.modules[__name__ + ".alternatingdirection"]
     return me

@@ -37,3 +37,19 @@ def test_estimate_is_between_extrapolations():
 def test_drop_in_refuses_fields_without_two_layers(shape):
     with pytest.raises(ValueError):
         ST.insulating_z_min_surface_temperature(np.zeros(shape), 1e-3)
+
+
+def test_installed_as_heatsim2_submodule():
+    """``import heatsim2.surface_temperature`` resolves to the drop-in after install_as_heatsim2()."""
+    import sys
+    import heatsim2_gb300
+    saved = {k: v for k, v in sys.modules.items() if k == "heatsim2" or k.startswith("heatsim2.")}
+    try:
+        heatsim2_gb300.install_as_heatsim2()
+        import heatsim2.surface_temperature as m
+        assert m is ST
+        assert m.insulating_z_min_surface_temperature is ST.insulating_z_min_surface_temperature
+    finally:
+        for k in [k for k in sys.modules if k == "heatsim2" or k.startswith("heatsim2.")]:
+            del sys.modules[k]
+        sys.modules.update(saved)
