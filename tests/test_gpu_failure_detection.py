@@ -2,7 +2,7 @@
 
 A bounded device wait that runs out reports HS2G_ERR_TIMEOUT and leaves the context usable (the same wait
 guards every mbarrier of the TMA sweeps); a device allocation that cannot succeed returns HS2G_ERR_NOMEM with
-nothing leaked; host-side validation errors are covered with the parity tests."""
+nothing leaked and the handle usable; host-side validation errors are covered with the parity tests."""
 import ctypes
 import time
 
@@ -50,14 +50,40 @@ def test_wait_limit_is_validated(cuda_ok):
 
 
 def test_device_allocation_failure_is_reported(cuda_ok):
+    """A forward pass whose checkpoint store cannot be allocated (2^21 states of 2^20 voxels, 16 TB: the first
+    cudaMalloc fails, nothing is partially filled) returns HS2G_ERR_NOMEM; the handle stays usable."""
     import torch
     L = _native.load()
     free0 = torch.cuda.mem_get_info()[0]
-    g = (_native.AdjointGrid * 1)(_native.AdjointGrid(4096, 4096, 4096, 1e-3, 1e-3, 1e-3))   # ~14 PB of fields
+    n, nsteps = 1 << 20, 1 << 21
+    g = (_native.AdjointGrid * 1)(_native.AdjointGrid(n, 1, 1, 1e-3, 1e-3, 1e-3))
     h = ctypes.c_void_p()
-    assert L.hs2g_adjoint_create(1, g, 0.01, 0, ctypes.byref(h)) == _native.ERR_NOMEM
-    assert not h.value
-    assert b"alloc" in L.hs2g_last_error().lower() or b"memory" in L.hs2g_last_error().lower()
+    assert L.hs2g_adjoint_create(1, g, 0.01, 0, ctypes.byref(h)) == _native.OK
+    try:
+        k, C, q = np.full(n, 50.0), np.full(n, 3.6e6), np.zeros(n)
+        assert L.hs2g_adjoint_set_parameters(h, k.ctypes.data, C.ctypes.data, q.ctypes.data, 0) == _native.OK
+        sched, obs, T0, loss = np.zeros(nsteps), np.zeros(nsteps), np.zeros(n), np.zeros(1)
+        rc = L.hs2g_adjoint_forward(h, nsteps, sched.ctypes.data, T0.ctypes.data, obs.ctypes.data, 1,
+                                    loss.ctypes.data, None, 0, None)
+        assert rc == _native.ERR_NOMEM
+        assert b"alloc" in L.hs2g_last_error().lower() or b"memory" in L.hs2g_last_error().lower()
+        # the same handle still runs a forward pass that fits
+        assert L.hs2g_adjoint_forward(h, 1, sched.ctypes.data, T0.ctypes.data, obs.ctypes.data, 1,
+                                      loss.ctypes.data, None, 0, None) == _native.OK
+        assert loss[0] == 0.0
+    finally:
+        L.hs2g_adjoint_destroy(h)
     torch.cuda.synchronize()
-    assert torch.cuda.mem_get_info()[0] >= free0 - (64 << 20)   # partial allocations were released
+    assert torch.cuda.mem_get_info()[0] >= free0 - (64 << 20)   # everything was released
+    _step_still_works()
+
+
+def test_oversized_adjoint_is_refused_before_allocating(cuda_ok):
+    """2^31 voxels or more (27 per-voxel FP64 fields: over 464 GB) are refused with HS2G_ERR_ARG."""
+    L = _native.load()
+    g = (_native.AdjointGrid * 1)(_native.AdjointGrid(4096, 4096, 4096, 1e-3, 1e-3, 1e-3))
+    h = ctypes.c_void_p()
+    assert L.hs2g_adjoint_create(1, g, 0.01, 0, ctypes.byref(h)) == _native.ERR_ARG
+    assert not h.value
+    assert b"2^31" in L.hs2g_last_error()
     _step_still_works()
