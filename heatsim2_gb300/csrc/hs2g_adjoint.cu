@@ -768,6 +768,7 @@ struct hs2g_adjoint {
   double* ckpts = nullptr;  // ceil(nsteps / ckpt) * n
   double* seg = nullptr;    // ckpt * 4 * n: T, y0, y1, y2 of each step of a segment
   double* seg2 = nullptr;   // a second segment store: the next segment is recomputed while this one is swept
+  int stored_seg = -1;      // the segment whose states the last forward pass left in its store (-1: none)
   cudaStream_t rec_stream = nullptr;  // the recompute stream
   cudaEvent_t ev_rec[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr}, ev_start = nullptr;
   double* T = nullptr;      // forward state
@@ -1084,6 +1085,7 @@ int hs2g_adjoint_set_parameters(hs2g_adjoint* a, const double* k, const double* 
   const cudaMemcpyKind kind = in_kind(flags);
   a->have_params = false;
   a->nsteps = 0;
+  a->stored_seg = -1;
   cudaError_t e = cudaMemcpyAsync(a->k, k, sizeof(double) * n, kind, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(a->C, C, sizeof(double) * n, kind, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(a->q, q, sizeof(double) * n, kind, st);
@@ -1126,15 +1128,34 @@ int hs2g_adjoint_forward(hs2g_adjoint* a, int nsteps, const double* schedule, co
   if (e == cudaSuccess) e = cudaMemcpyAsync(a->T, T0, sizeof(double) * n, in_kind(flags), st);
   if (e == cudaSuccess) e = cudaEventRecord(a->ev0, st);
   a->sched.assign(schedule, schedule + nsteps);
+  a->stored_seg = -1;
+  // The last segment's states (T, y0, y1, y2 of each step, the layout the recompute writes) go straight into
+  // the segment store the backward pass sweeps first, when the stores already exist from an earlier backward
+  // pass: that pass then skips its first recompute, the one nothing overlaps.  The same kernels compute the
+  // same states, so the gradients do not change.
+  const int64_t seg_need = (int64_t)ckpt * 4 * n;
+  double* store = nullptr;
+  if (a->seg && a->seg_cap >= seg_need && (nck == 1 || (a->seg2 && a->seg2_cap >= seg_need)))
+    store = ((nck - 1) & 1) ? a->seg2 : a->seg;
+  const int s_store = store ? (int)((nck - 1) * ckpt) : nsteps;
   const hs2g::AView v = view(a);
   for (int s = 0; s < nsteps && e == cudaSuccess; ++s) {
     if (s % ckpt == 0)
       e = cudaMemcpyAsync(a->ckpts + (int64_t)(s / ckpt) * n, a->T, sizeof(double) * n, cudaMemcpyDeviceToDevice,
                           st);
-    // the adjoint buffers are free during the forward pass and hold the increments
-    if (e == cudaSuccess) e = fwd_step(a, st, a->T, a->T, a->mu[0], a->mu[1], a->mu[2], a->sched[s]);
+    double* out = a->T;
+    if (s < s_store) {
+      // the adjoint buffers are free during the forward pass and hold the increments
+      if (e == cudaSuccess) e = fwd_step(a, st, a->T, a->T, a->mu[0], a->mu[1], a->mu[2], a->sched[s]);
+    } else {
+      double* slot = store + (int64_t)(s - s_store) * 4 * n;
+      if (s == s_store && e == cudaSuccess)
+        e = cudaMemcpyAsync(slot, a->T, sizeof(double) * n, cudaMemcpyDeviceToDevice, st);
+      if (s + 1 < nsteps) out = slot + 4 * n;
+      if (e == cudaSuccess) e = fwd_step(a, st, slot, out, slot + n, slot + 2 * n, slot + 3 * n, a->sched[s]);
+    }
     if (e == cudaSuccess) {
-      hs2g::adj_misfit_kernel<<<dim3(hs2g::kMisfitBlocks, a->ninst), 256, 0, st>>>(v, a->T, a->obs, s, a->parts);
+      hs2g::adj_misfit_kernel<<<dim3(hs2g::kMisfitBlocks, a->ninst), 256, 0, st>>>(v, out, a->obs, s, a->parts);
       e = cudaGetLastError();
     }
   }
@@ -1159,6 +1180,7 @@ int hs2g_adjoint_forward(hs2g_adjoint* a, int nsteps, const double* schedule, co
   }
   a->nsteps = nsteps;
   a->ckpt = ckpt;
+  a->stored_seg = store ? (int)(nck - 1) : -1;
   return HS2G_OK;
 }
 
@@ -1182,6 +1204,9 @@ int hs2g_adjoint_backward(hs2g_adjoint* a, double* gk, double* gC, double* gq, d
     if (!dbl) cudaGetLastError();  // out of memory for the second store: recompute and sweep in turn
   }
   double* bufs[2] = {a->seg, dbl ? a->seg2 : a->seg};
+  // the last forward pass may have left the last segment in its store (see hs2g_adjoint_forward)
+  const bool stored = a->stored_seg == nseg - 1 && (nseg == 1 || dbl);
+  a->stored_seg = -1;
   e = cudaEventRecord(a->ev0, st);
   double* zero_list[] = {a->gg[0], a->gg[1], a->gg[2], a->gM, a->gq};
   for (double* p : zero_list)
@@ -1206,14 +1231,14 @@ int hs2g_adjoint_backward(hs2g_adjoint* a, double* gk, double* gC, double* gq, d
     if (r == cudaSuccess && dbl) r = cudaEventRecord(a->ev_rec[sg & 1], rs);
     return r;
   };
-  if (e == cudaSuccess) e = recompute(nseg - 1);
+  if (e == cudaSuccess && !stored) e = recompute(nseg - 1);
   for (int sg = nseg - 1; sg >= 0 && e == cudaSuccess; --sg) {
     if (dbl && sg >= 1) {
       // store (sg-1)&1 was last read by the sweep of segment sg+1
       e = cudaStreamWaitEvent(rs, a->ev_done[(sg - 1) & 1], 0);
       if (e == cudaSuccess) e = recompute(sg - 1);
     }
-    if (e == cudaSuccess && dbl) e = cudaStreamWaitEvent(st, a->ev_rec[sg & 1], 0);
+    if (e == cudaSuccess && dbl && !(stored && sg == nseg - 1)) e = cudaStreamWaitEvent(st, a->ev_rec[sg & 1], 0);
     const int s0 = sg * C, s1 = std::min(N, s0 + C);
     const double* buf = bufs[sg & 1];
     for (int s = s1 - 1; s >= s0 && e == cudaSuccess; --s) {

@@ -75,6 +75,24 @@ def test_checkpoint_interval_changes_nothing(cuda_ok):
                 np.testing.assert_array_equal(x, y)
 
 
+def test_repeated_evaluations_on_one_handle(cuda_ok):
+    """From the second evaluation on, the forward pass leaves its last segment in the backward pass's store and
+    the backward pass skips recomputing it; gradients stay equal bit for bit to a fresh handle's, also when the
+    checkpoint interval changes between evaluations (one segment, more, an interval whose store is too small)."""
+    dt, N = 0.01, 23
+    p = _problem(3, (5, 9, 11), N)
+    a = Adjoint([(p["shape"], p["spacing"])], dt)
+    a.set_parameters(p["k"], p["C"], p["q"])
+    for ckpt in (4, 4, 23, 7, 1, 10, 5):
+        fresh, lf = _adjoint(p, dt, ckpt)
+        gf = fresh.backward()
+        la = a.forward(p["T0"], p["obs"], p["schedule"], ckpt)
+        ga = a.backward()
+        np.testing.assert_array_equal(la, lf)
+        for x, y in zip(ga, gf):
+            np.testing.assert_array_equal(x, y)
+
+
 def test_batch_equals_single_instances(cuda_ok):
     """Uneven instances in one concatenated state give, per instance, the single-instance loss and gradients
     bit for bit."""
