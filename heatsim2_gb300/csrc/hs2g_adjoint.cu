@@ -356,8 +356,9 @@ __global__ void __launch_bounds__(128, kYMinBlocks) adj_ysolve_kernel(AView v, i
 // What bounds it is the recurrence warp's own instruction stream (about 6 cycles per instruction with
 // nothing to interleave), not memory: at 32x128x128 the 128-row y solve took 38 us with one warp issuing both
 // the copies and the recurrence, 26 us with the copies left out (a timing probe) and takes 31 us with the
-// copies on a second warp.  Eight ring stages or 16-row stages were slower, staging each block's operands in
-// registers changed nothing, and spreading the lines over four 8-lane warps doubled the z time.
+// copies on a second warp (a third warp sharing the copies: unchanged).  Eight ring stages or 16-row stages
+// were slower, staging each block's operands in registers changed nothing, and spreading the lines over four
+// 8-lane warps doubled the z time.
 constexpr int kFS = 4;            // ring stages
 constexpr int kFR = 8;            // rows per stage
 constexpr int kFewMaxLen = 512;   // longest line the few-line kernels hold (128 KB of line values)
