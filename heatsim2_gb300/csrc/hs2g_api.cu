@@ -20,6 +20,11 @@ using hs2g::Dims;
 // its columns.  The host link (~0.2 TB/s each way on GB300) is then busy while the sweeps run.
 constexpr int kCopyChunks = 4;
 constexpr double kSlabEnd[kCopyChunks] = {0.55, 0.80, 0.93, 1.0};  // upload slab c ends at this fraction of nz
+// x-lines per CTA of each slab's x sweep: a small launch lasts as long as one CTA's chunk loop, so the later,
+// smaller slabs take smaller CTAs and finish sooner after their upload (64x512x512 composite panel: 1.77 ms
+// per host-buffer step against 1.85 ms with 32 lines throughout; 16 for every slab 1.80, 8 for the last two
+// 1.83)
+constexpr int kSlabLines[kCopyChunks] = {32, 32, 16, 8};
 constexpr int64_t kPipelineMinVoxels = int64_t(1) << 20;
 
 struct hs2g_handle {
@@ -304,7 +309,7 @@ int step_host_pipelined(hs2g_handle* h, hs2g::StepArgs& a, const hs2g::QTable& q
     HS2G_CUDA(cudaStreamWaitEvent(xs, h->ev_begin, 0), "upload T");
     HS2G_CUDA(cudaStreamWaitEvent(xs, h->ev_in[c], 0), "upload T");
     const int64_t upto = (k1 == d.nz ? d.nz : k1 - 1) * d.ny;
-    cudaError_t e = hs2g::launch_x_range(a, h->c, q, done, upto, xs);
+    cudaError_t e = hs2g::launch_x_range(a, h->c, q, done, upto, kSlabLines[c], xs);
     if (e != cudaSuccess) return cuda_fail(e, "x sweep");
     HS2G_CUDA(cudaEventRecord(h->ev_x[c], xs), "x sweep");
     HS2G_CUDA(cudaStreamWaitEvent(s, h->ev_x[c], 0), "x sweep");

@@ -103,9 +103,10 @@ cudaError_t launch_surface_estimate(int64_t nxy, const double* T, double dz, dou
 // one bounded mbarrier wait on a barrier that receives its arrival (arrive != 0) or none (hs2g_lines.cu)
 cudaError_t wait_selftest(uint64_t limit_ns, int arrive, int* status_dev, cudaStream_t s);
 // the step in pieces, for overlapping host copies with it: the x sweep over x-lines [line_begin, line_end)
-// (line = k*ny + j), the whole y sweep, the plain z sweep over columns [col_begin, col_end) (col = j*nx + i)
+// (line = k*ny + j) with 32, 16 or 8 x-lines per CTA, the whole y sweep, the plain z sweep over columns
+// [col_begin, col_end) (col = j*nx + i)
 cudaError_t launch_x_range(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_begin,
-                           int64_t line_end, cudaStream_t s);
+                           int64_t line_end, int lines_per_cta, cudaStream_t s);
 cudaError_t launch_y(const StepArgs& a, const Coeffs& c, cudaStream_t s);
 cudaError_t launch_z_range(const StepArgs& a, const Coeffs& c, int64_t col_begin, int64_t col_end, cudaStream_t s);
 

@@ -74,22 +74,25 @@ __device__ __forceinline__ double stencil_x(const Dims& d, const double* __restr
 
 // RANGED: the launch covers x-lines [line_begin, line_end) (the overlapped host-buffer step); otherwise all
 // nz*ny lines, with the arguments unused -- the two are separate instances so that the whole-grid kernel keeps
-// its own register allocation.
-template <bool HAS_Q, bool RANGED>
+// its own register allocation.  LINES x-lines per CTA: 32 for the whole grid; the host-buffer step's later,
+// smaller slabs take 16 or 8, whose CTAs finish sooner (a CTA's chunk loop, not the GPU's throughput, sets
+// how long a small launch takes).
+template <bool HAS_Q, bool RANGED, int LINES = kXLines>
 __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d, const double* __restrict__ T, Coeffs c,
                                                              const uint8_t* __restrict__ vclass,
                                                              const double* __restrict__ qdense, QTable qt,
                                                              double* __restrict__ W0, int64_t line_begin,
                                                              int64_t line_end) {
-  __shared__ double sr[kXLines][kXChunk + 1];
-  __shared__ double sa[kXLines][kXChunk + 1];
+  constexpr int kPerWarp = LINES / kXWarps;
+  __shared__ double sr[LINES][kXChunk + 1];
+  __shared__ double sa[LINES][kXChunk + 1];
   __shared__ double sq[HAS_Q ? HS2G_MAX_CLASSES : 1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (HAS_Q) {
     for (int e = threadIdx.x; e < HS2G_MAX_CLASSES; e += kXThreads) sq[e] = qt.q[e];
   }
   const int64_t nlines = RANGED ? line_end : d.nz * d.ny;
-  const int64_t L0 = (RANGED ? line_begin : 0) + (int64_t)blockIdx.x * kXLines;
+  const int64_t L0 = (RANGED ? line_begin : 0) + (int64_t)blockIdx.x * LINES;
   const int nchunks = (int)((d.nx + kXChunk - 1) / kXChunk);
   __syncthreads();
 
@@ -98,8 +101,8 @@ __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d,
   for (int ch = 0; ch < nchunks; ++ch) {
     const int64_t i = (int64_t)ch * kXChunk + lane;
 #pragma unroll
-    for (int ll = 0; ll < kXLinesPerWarp; ++ll) {
-      const int l = warp * kXLinesPerWarp + ll;
+    for (int ll = 0; ll < kPerWarp; ++ll) {
+      const int l = warp * kPerWarp + ll;
       const int64_t L = L0 + l;
       double r = 0.0, a = 0.0;
       if (L < nlines && i < d.nx) {
@@ -110,7 +113,7 @@ __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d,
       sa[l][lane] = a;
     }
     __syncthreads();
-    if (warp * 32 + lane < kXLines) {  // lane = line of the recurrence
+    if (warp * 32 + lane < LINES) {  // lane = line of the recurrence
       const int l = warp * 32 + lane;
       const int cw = (int)min((int64_t)kXChunk, d.nx - (int64_t)ch * kXChunk);
       double z = carry;
@@ -122,8 +125,8 @@ __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d,
     }
     __syncthreads();
 #pragma unroll
-    for (int ll = 0; ll < kXLinesPerWarp; ++ll) {
-      const int l = warp * kXLinesPerWarp + ll;
+    for (int ll = 0; ll < kPerWarp; ++ll) {
+      const int l = warp * kPerWarp + ll;
       const int64_t L = L0 + l;
       if (L < nlines && i < d.nx) W0[L * d.nx + i] = sr[l][lane];
     }
@@ -135,8 +138,8 @@ __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d,
   for (int ch = nchunks - 1; ch >= 0; --ch) {
     const int64_t i = (int64_t)ch * kXChunk + lane;
 #pragma unroll
-    for (int ll = 0; ll < kXLinesPerWarp; ++ll) {
-      const int l = warp * kXLinesPerWarp + ll;
+    for (int ll = 0; ll < kPerWarp; ++ll) {
+      const int l = warp * kPerWarp + ll;
       const int64_t L = L0 + l;
       double z = 0.0, b = 0.0;
       if (L < nlines && i < d.nx) {
@@ -148,7 +151,7 @@ __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d,
       sa[l][lane] = b;
     }
     __syncthreads();
-    if (warp * 32 + lane < kXLines) {
+    if (warp * 32 + lane < LINES) {
       const int l = warp * 32 + lane;
       const int cw = (int)min((int64_t)kXChunk, d.nx - (int64_t)ch * kXChunk);
       double x = carry;
@@ -160,8 +163,8 @@ __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d,
     }
     __syncthreads();
 #pragma unroll
-    for (int ll = 0; ll < kXLinesPerWarp; ++ll) {
-      const int l = warp * kXLinesPerWarp + ll;
+    for (int ll = 0; ll < kPerWarp; ++ll) {
+      const int l = warp * kPerWarp + ll;
       const int64_t L = L0 + l;
       if (L < nlines && i < d.nx) W0[L * d.nx + i] = sr[l][lane];
     }
@@ -321,17 +324,28 @@ cudaError_t launch_step(const StepArgs& a, const Coeffs& c, const QTable& q, cud
   return launch_step_events(a, c, q, s, nullptr);
 }
 
-cudaError_t launch_x_range(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_begin,
-                           int64_t line_end, cudaStream_t s) {
+template <int LINES>
+void launch_x_lines(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_begin, int64_t line_end,
+                    cudaStream_t s) {
   const Dims& d = a.d;
-  if (line_end <= line_begin) return cudaSuccess;
-  const unsigned gx = blocks(line_end - line_begin, kXLines);
+  const unsigned gx = blocks(line_end - line_begin, LINES);
   if (a.has_qtab || a.qdense != nullptr)
-    sweep_x_kernel<true, true><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0, line_begin,
-                                                        line_end);
+    sweep_x_kernel<true, true, LINES><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0,
+                                                               line_begin, line_end);
   else
-    sweep_x_kernel<false, true><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0, line_begin,
-                                                         line_end);
+    sweep_x_kernel<false, true, LINES><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0,
+                                                                line_begin, line_end);
+}
+
+cudaError_t launch_x_range(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_begin,
+                           int64_t line_end, int lines_per_cta, cudaStream_t s) {
+  if (line_end <= line_begin) return cudaSuccess;
+  if (lines_per_cta == 8)
+    launch_x_lines<8>(a, c, q, line_begin, line_end, s);
+  else if (lines_per_cta == 16)
+    launch_x_lines<16>(a, c, q, line_begin, line_end, s);
+  else
+    launch_x_lines<kXLines>(a, c, q, line_begin, line_end, s);
   return cudaGetLastError();
 }
 
