@@ -181,7 +181,9 @@ def _is_torch_cuda(x):
 
 
 def _class_map_update(P, volumetric_elements):
-    """The host source-class map to upload when it differs from the one on the device, else None."""
+    """The host source-class map to upload when it differs from the one on the device, else None.  The caller
+    records it as the device's map (``_class_map_uploaded``) only once the native call that uploads it has
+    succeeded, so a failed call leaves the map to be uploaded again."""
     if volumetric_elements is None or volumetric_elements is P.compiled_volumetric:
         return None
     ve = np.ascontiguousarray(volumetric_elements, dtype=np.uint8)
@@ -189,8 +191,12 @@ def _class_map_update(P, volumetric_elements):
         raise ValueError("volumetric_elements has shape %s, expected %s" % (ve.shape, tuple(P.shape)))
     if np.array_equal(ve, P.compiled_volumetric):
         return None
-    P.compiled_volumetric = ve.copy()
-    return P.compiled_volumetric
+    return ve.copy()
+
+
+def _class_map_uploaded(P, newmap):
+    if newmap is not None:
+        P.compiled_volumetric = newmap
 
 
 def run_adi_steps(ADI_params, ADI_steps, t, dt, Tarray, volumetric_elements, volumetric):
@@ -222,6 +228,7 @@ def run_adi_steps(ADI_params, ADI_steps, t, dt, Tarray, volumetric_elements, vol
         _native.check(L.hs2g_step(P.handle.ptr, T.data_ptr(), out.data_ptr(), qptr,
                                   qd.data_ptr() if qd is not None else None,
                                   newmap.ctypes.data if newmap is not None else None, _native.DEVICE))
+        _class_map_uploaded(P, newmap)
         if qd is not None:
             qd.record_stream(stream)
         return out
@@ -233,6 +240,7 @@ def run_adi_steps(ADI_params, ADI_steps, t, dt, Tarray, volumetric_elements, vol
     _native.check(L.hs2g_step(P.handle.ptr, T.ctypes.data, out.ctypes.data, qptr,
                               qdense.ctypes.data if qdense is not None else None,
                               newmap.ctypes.data if newmap is not None else None, 0))
+    _class_map_uploaded(P, newmap)
     return out
 
 
@@ -297,6 +305,8 @@ def run(ADI_params, Tarray, times, dt, volumetric_elements, volumetric, record_l
             _native.check(L.hs2g_step(P.handle.ptr, ptr, ptr, qtabs[s].ctypes.data, qdp,
                                       newmap.ctypes.data if (first and newmap is not None) else None,
                                       flags | _native.SYNC))
+            if first:
+                _class_map_uploaded(P, newmap)
             if hist is not None:
                 if record_surface:
                     from .surface_temperature import insulating_z_min_surface_temperature

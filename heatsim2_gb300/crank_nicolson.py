@@ -29,8 +29,9 @@ _K_LO, _K_HI = "kmat_lo", "kmat_hi"
 
 
 class UnalignedAnisotropyError(AssertionError, NotImplementedError):
-    """Raised where the reference's stage split asserts (alternatingdirection_c_pyx.pyx:570): a face flux
-    couples temperatures across axes, which the three-stage ADI step cannot solve."""
+    """Raised where the reference asserts: a face flux couples temperatures across axes, which the three-stage
+    ADI step cannot solve (alternatingdirection_c_pyx.pyx:570), or ``unaligned_anisotropic=True`` was asked
+    for, whose stage-count assertion fails in the reference for every problem (pyx:452)."""
 
 
 def _form_from_coeffs(coeffs):
@@ -209,9 +210,6 @@ class ClassProblem(object):
                     raise ValueError("surface curvatures must be finite")
                 curv.append(np.ascontiguousarray(c))
             self.curvature = tuple(curv)
-        if unaligned_anisotropic:
-            raise NotImplementedError("the unaligned-anisotropic ADI mode (alternatingdirection_c_pyx.pyx:511-564) "
-                                      "is not provided")
         nz, ny, nx = int(nz), int(ny), int(nx)
         if nz < 1 or ny < 1 or nx < 1:
             raise ValueError("grid dimensions must be positive")
@@ -232,6 +230,16 @@ class ClassProblem(object):
         self.mats = compile_materials(materials, dt)
         self.forms = compile_boundary_forms(boundaries, dz, dy, dx)
         self.boundaries = boundaries
+        if unaligned_anisotropic:
+            # The reference's unaligned-anisotropic mode splits every voxel's heat balance into 15 stages
+            # (alternatingdirection_c_pyx.pyx:511-564) but its adi_setup builds three stage matrices
+            # (pyx:418-445), so the stage-count assertion of add_equation_to_adi_matrices (pyx:452) fails at
+            # the first voxel of every problem, after the classes have been evaluated.  Same error here.
+            raise UnalignedAnisotropyError(
+                "unaligned_anisotropic=True: the reference's setup fails its stage-count assertion "
+                "(alternatingdirection_c_pyx.pyx:452: 15 stage expressions for 3 stage matrices) for every "
+                "problem, so this mode has no results to reproduce; anisotropy aligned with the grid axes runs "
+                "with unaligned_anisotropic=False")
         self.struct = _native.ClassProblem(nz, ny, nx, len(materials), len(boundaries), self.mats, self.forms,
                                            self.mat.ctypes.data, self.bz.ctypes.data, self.by.ctypes.data,
                                            self.bx.ctypes.data, self.vol.ctypes.data)
@@ -254,7 +262,8 @@ def setup(z0, y0, x0, dz, dy, dx, nz, ny, nx, dt, materials, boundaries, volumet
 
     Arguments as in the reference (crank_nicolson.pyx:128-142).  With surface curvatures the problem compiles
     in the reference's curved-surface mode (heatsim2_gb300.curvature; ``ADI_params.volume_array`` is then the
-    per-cell volume).  The unaligned-anisotropic 15-stage mode is not provided (NotImplementedError)."""
+    per-cell volume).  ``unaligned_anisotropic=True`` raises AssertionError after the classes are validated, as
+    the reference's setup does for every problem (alternatingdirection_c_pyx.pyx:452)."""
     from .alternatingdirection import adi_params, adi_step
     cp = ClassProblem(z0, y0, x0, dz, dy, dx, nz, ny, nx, dt, materials, boundaries, volumetric, material_elements,
                       boundary_z_elements, boundary_y_elements, boundary_x_elements, volumetric_elements,

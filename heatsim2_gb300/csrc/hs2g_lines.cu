@@ -25,6 +25,7 @@
 #include <utility>
 
 #include "hs2g_internal.cuh"
+#include "hs2g_ring.h"
 
 namespace hs2g {
 namespace {
@@ -142,8 +143,7 @@ __global__ void __launch_bounds__(kNL) line_sweep_tma_kernel(Geometry g, const _
   }
   __syncthreads();
 
-  uint32_t parity = 0;   // bit s: parity of the next completion of slot s
-  uint32_t pending = 0;  // producer: slots with copies issued and not yet waited for
+  SlotRing ring;  // slot phases; pending slots are tracked by the producer (tid 0), which issues every copy
   const int cx = (int)i0, cz = (int)plane;
 
   auto issue_fwd = [&](int64_t q) {  // tile q covers rows [q*kRows, q*kRows + kRows)
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(kNL) line_sweep_tma_kernel(Geometry g, const _
     mbar_expect_tx(&bars[s], 2u * kTileBytes);
     tile_load(tile(s, 0), &mA, cx, r0, cz, &bars[s]);
     tile_load(tile(s, 1), &mAlpha, cx, r0, cz, &bars[s]);
-    pending |= 1u << s;
+    ring.issued(s);
   };
   auto issue_back = [&](int64_t q) {  // back tile q covers rows [n - (q+1)*kRows, n - q*kRows)
     const int s = (int)(q % kSlots);
@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(kNL) line_sweep_tma_kernel(Geometry g, const _
     tile_load(tile(s, 0), &mScratch, cx, r0, cz, &bars[s]);
     tile_load(tile(s, 1), &mBeta, cx, r0, cz, &bars[s]);
     if (ADD_T) tile_load(tile(s, 2), &mT, cx, r0, cz, &bars[s]);
-    pending |= 1u << s;
+    ring.issued(s);
   };
 
   bool aborted = false;
@@ -171,9 +171,9 @@ __global__ void __launch_bounds__(kNL) line_sweep_tma_kernel(Geometry g, const _
   double z = 0.0;
   for (int64_t q = 0; q < ntiles && !aborted; ++q) {
     const int s = (int)(q % kSlots);
-    if (!mbar_wait_bounded(&bars[s], (parity >> s) & 1u)) *abort_flag = 1;
-    parity ^= 1u << s;
-    if (tid == 0) pending &= ~(1u << s);
+    const bool done = mbar_wait_bounded(&bars[s], ring.phase(s));
+    if (!done) *abort_flag = 1;
+    ring.waited(s, done);
     const double* tA = tile(s, 0);
     const double* tAl = tile(s, 1);
     const int64_t r0 = q * kRows;
@@ -201,9 +201,9 @@ __global__ void __launch_bounds__(kNL) line_sweep_tma_kernel(Geometry g, const _
   double x = 0.0;
   for (int64_t q = 0; q < ntiles && !aborted; ++q) {
     const int s = (int)(q % kSlots);
-    if (!mbar_wait_bounded(&bars[s], (parity >> s) & 1u)) *abort_flag = 1;
-    parity ^= 1u << s;
-    if (tid == 0) pending &= ~(1u << s);
+    const bool done = mbar_wait_bounded(&bars[s], ring.phase(s));
+    if (!done) *abort_flag = 1;
+    ring.waited(s, done);
     const double* tZ = tile(s, 0);
     const double* tB = tile(s, 1);
     const double* tT = tile(s, ADD_T ? 2 : 0);
@@ -223,9 +223,10 @@ __global__ void __launch_bounds__(kNL) line_sweep_tma_kernel(Geometry g, const _
     if (!aborted && tid == 0 && q + kSlots < ntiles) issue_back(q + kSlots);
   }
   if (aborted && tid == 0) {
-    // drain: wait (bounded) for every copy still in flight into this CTA's shared memory
+    // drain: wait (bounded) for every copy still in flight into this CTA's shared memory, including a slot
+    // whose wait above gave up (its phase was not advanced)
     for (int s = 0; s < kSlots; ++s)
-      if (pending & (1u << s)) mbar_wait_bounded(&bars[s], (parity >> s) & 1u);
+      if (ring.in_flight(s)) mbar_wait_bounded(&bars[s], ring.phase(s));
     atomicExch(status, HS2G_ERR_TIMEOUT);
   }
 }

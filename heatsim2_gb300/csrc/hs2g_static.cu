@@ -13,13 +13,22 @@
 // it later reads.  Calls that overlap on the GPU (on different streams, or from different host threads)
 // race on the array and must be serialised by the caller.
 //
-// The array's host-side name is only a stand-in for it; its device address is taken once per device with
-// cudaGetSymbolAddress, on the first call made with that device current.  Make that first call before any
-// stream capture.
+// The array's host-side name is only a stand-in for it; its device address is taken with
+// cudaGetSymbolAddress on the first call made with a device current, and again after that device's context
+// changed (a cudaDeviceReset reloads the module at a new address).  Make that first call before any stream
+// capture.
+//
+// The call validates what the kernels read: every computed voxel's capacity must be positive and finite.
+// The kernels record the first bad voxel in a device status word next to the array, and the call waits for
+// them (it synchronises `stream`) to return HS2G_ERR_CAPACITY; the output is then not a valid step.
 //
 // Arithmetic: the Douglas delta form of the step, (M - Lx/2) dT0 = L T + Q, (M - Ly/2) dT1 = M dT0,
 // (M - Lz/2) dT2 = M dT1, T' = T + dT2, each line solved by the Thomas algorithm in the reference's
 // normalisation (tridiag.pyx:25-41, :58-67) with the pivots formed as the line is swept.  One thread per line.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstdio>
 #include <mutex>
 
 #include "hs2g_internal.cuh"
@@ -31,6 +40,8 @@ constexpr int kMaxDevices = 64;
 
 // dT0 / dT2 forward values, dT1, and the current sweep's normalised super-diagonal u = hi / pivot
 __device__ __align__(256) double g_static_scratch[3 * kStaticVoxels];
+// first invalid voxel seen by the kernels of the current call (hs2g::record_error encoding), 0 when none
+__device__ unsigned long long g_static_status;
 
 struct StaticView {
   double* w0;
@@ -62,6 +73,7 @@ __global__ void static_x_kernel(Problem P, const double* __restrict__ T, StaticV
     const int64_t p = L * d.nx + i;
     double dd = 1.0, lo = 0.0, hi = 0.0, r = 0.0;
     if (computed(P, p)) {
+      if (!(P.M[p] > 0.0 && P.M[p] < INFINITY)) hs2g::record_error(&g_static_status, HS2G_ERR_CAPACITY, 3, p);
       const int64_t fx = L * (d.nx + 1) + i, fy = (k * (d.ny + 1) + j) * d.nx + i;
       const double t = T[p];
       const double gxl = i > 0 ? P.Gx[fx] : 0.0, gxh = i + 1 < d.nx ? P.Gx[fx + 1] : 0.0;
@@ -156,22 +168,55 @@ __global__ void static_z_kernel(Problem P, const double* T_in, double* T_out, St
 }
 
 std::mutex g_static_mutex;
-double* g_static_ptr[kMaxDevices] = {nullptr};
 
-// Device address of the scratch array on the current device, taken once per device.
-cudaError_t static_scratch(double** out) {
+// The scratch array's and the status word's device addresses, per device, with the context they were taken in.
+struct StaticAddress {
+  CUcontext ctx = nullptr;
+  double* scratch = nullptr;
+  unsigned long long* status = nullptr;
+};
+StaticAddress g_static_addr[kMaxDevices];
+
+PFN_cuCtxGetCurrent_v4000 ctx_get_current_fn() {
+  static PFN_cuCtxGetCurrent_v4000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, []() {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+  });
+  return fn;
+}
+
+// Set-up: device addresses of the scratch array and the status word on the current device, taken with
+// cudaGetSymbolAddress the first time and whenever the device's current context is no longer the one they were
+// taken in.
+cudaError_t static_addresses(StaticAddress* out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  PFN_cuCtxGetCurrent_v4000 get_ctx = ctx_get_current_fn();
+  CUcontext ctx = nullptr;
+  if (!get_ctx || get_ctx(&ctx) != CUDA_SUCCESS) return cudaErrorInitializationError;
   std::lock_guard<std::mutex> lock(g_static_mutex);
-  if (!g_static_ptr[dev]) {
-    void* ptr = nullptr;
-    e = cudaGetSymbolAddress(&ptr, g_static_scratch);
+  StaticAddress& a = g_static_addr[dev];
+  if (!ctx || !a.scratch || a.ctx != ctx) {
+    // (with no context current yet, the first runtime call below creates the device's primary context)
+    void* scratch = nullptr;
+    void* status = nullptr;
+    e = cudaGetSymbolAddress(&scratch, g_static_scratch);
     if (e != cudaSuccess) return e;
-    g_static_ptr[dev] = static_cast<double*>(ptr);
+    e = cudaGetSymbolAddress(&status, g_static_status);
+    if (e != cudaSuccess) return e;
+    if (!ctx && (get_ctx(&ctx) != CUDA_SUCCESS || !ctx)) return cudaErrorInitializationError;
+    a.ctx = ctx;
+    a.scratch = static_cast<double*>(scratch);
+    a.status = static_cast<unsigned long long*>(status);
   }
-  *out = g_static_ptr[dev];
+  *out = a;
   return cudaSuccess;
 }
 
@@ -187,17 +232,48 @@ extern "C" int hs2g_step_static(int64_t nz, int64_t ny, int64_t nx, const double
     return hs2g::set_last_error(HS2G_ERR_ARG,
                                 "hs2g_step_static: grid larger than HS2G_STATIC_MAX_VOXELS (1048576) voxels; "
                                 "use hs2g_create_dense + hs2g_step");
-  double* base = nullptr;
-  if (static_scratch(&base) != cudaSuccess)
-    return hs2g::set_last_error(HS2G_ERR_CUDA, "hs2g_step_static: cannot take the scratch array's device address");
-  StaticView s{base, base + kStaticVoxels, base + 2 * kStaticVoxels};
+  char msg[256];
+  StaticAddress a;
+  cudaError_t e = static_addresses(&a);
+  if (e != cudaSuccess) {
+    snprintf(msg, sizeof(msg), "hs2g_step_static: cannot take the scratch array's device address: %s",
+             cudaGetErrorString(e));
+    return hs2g::set_last_error(HS2G_ERR_CUDA, msg);
+  }
+  StaticView s{a.scratch, a.scratch + kStaticVoxels, a.scratch + 2 * kStaticVoxels};
   Problem P{hs2g::Dims{nz, ny, nx}, Gz, Gy, Gx, capacity, fixed, Q};
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int th = 128;
-  static_x_kernel<<<(unsigned)((nz * ny + th - 1) / th), th, 0, st>>>(P, T_in, s);
-  static_y_kernel<<<(unsigned)((nz * nx + th - 1) / th), th, 0, st>>>(P, s);
-  static_z_kernel<<<(unsigned)((ny * nx + th - 1) / th), th, 0, st>>>(P, T_in, T_out, s);
-  if (cudaGetLastError() != cudaSuccess)
-    return hs2g::set_last_error(HS2G_ERR_CUDA, "hs2g_step_static: kernel launch failed");
+  // a launch error below must be this call's: drop a non-sticky error the caller left pending (a sticky error
+  // of an earlier failure in the context is reported by the launches themselves)
+  cudaGetLastError();
+  e = cudaMemsetAsync(a.status, 0, sizeof(unsigned long long), st);
+  if (e == cudaSuccess) {
+    static_x_kernel<<<(unsigned)((nz * ny + th - 1) / th), th, 0, st>>>(P, T_in, s);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) {
+    static_y_kernel<<<(unsigned)((nz * nx + th - 1) / th), th, 0, st>>>(P, s);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) {
+    static_z_kernel<<<(unsigned)((ny * nx + th - 1) / th), th, 0, st>>>(P, T_in, T_out, s);
+    e = cudaGetLastError();
+  }
+  unsigned long long status = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&status, a.status, sizeof(status), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    snprintf(msg, sizeof(msg), "hs2g_step_static: %s (%s)", cudaGetErrorName(e), cudaGetErrorString(e));
+    return hs2g::set_last_error(HS2G_ERR_CUDA, msg);
+  }
+  if (status) {
+    const int64_t p = (int64_t)(status & ((1ull << 54) - 1));
+    snprintf(msg, sizeof(msg),
+             "hs2g_step_static: computed voxel [%lld,%lld,%lld] has rho*c/dt <= 0 or not finite; the output is "
+             "not a valid step",
+             (long long)(p / (ny * nx)), (long long)((p / nx) % ny), (long long)(p % nx));
+    return hs2g::set_last_error(HS2G_ERR_CAPACITY, msg);
+  }
   return HS2G_OK;
 }

@@ -219,8 +219,12 @@ int hs2g_source_table(int nsrc, const int32_t* kind, const double* params, doubl
  * The intermediate fields live in a static device array sized for HS2G_STATIC_MAX_VOXELS voxels (24 MiB),
  * held by every GPU that loads the library until the process exits; larger grids return HS2G_ERR_ARG.
  * Every call shares that array: calls that overlap on the GPU race and must be serialised by the caller.
- * The first call on a device takes the array's device address (cudaGetSymbolAddress); make it before any
- * stream capture.  Work is queued on `stream` (a cudaStream_t, NULL = default stream); no synchronisation.
+ * The first call on a device takes the array's device address (cudaGetSymbolAddress), and so does the first
+ * call after the device's context changed (cudaDeviceReset); make that call before any stream capture.
+ * Work runs on `stream` (a cudaStream_t, NULL = default stream) and the call waits for it: a computed voxel
+ * whose capacity is not positive and finite returns HS2G_ERR_CAPACITY (the output is then not a valid step).
+ * A launch failure returns HS2G_ERR_CUDA; a sticky error left in the context by earlier work (an illegal
+ * address, say) surfaces here too, because every later launch in that context fails.
  */
 #define HS2G_STATIC_MAX_VOXELS (1 << 20)
 int hs2g_step_static(int64_t nz, int64_t ny, int64_t nx, const double* Gz, const double* Gy, const double* Gx,

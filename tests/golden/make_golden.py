@@ -3,7 +3,7 @@
 Run in a container where the reference sources are mounted (the reference is built into oracle/_ref by
 oracle/build_ref.py first):
 
-    python oracle/build_ref.py && python tests/golden/make_golden.py [curved | surface]
+    python oracle/build_ref.py && python tests/golden/make_golden.py [curved | surface | composite128 | unaligned]
 
 Each fixture ``<name>.npz`` holds the problem spec (heatsim2_gb300.workloads serialisation), the t values
 passed to the reference's run_adi_steps, and the temperature field the reference returned after selected
@@ -109,12 +109,64 @@ def surface_fixture(hs):
     print("wrote surface_temperature")
 
 
+def composite_panel_128(hs):
+    """The benchmark's composite panel recipe (anisotropic composite over aluminium, fixed ambient layer behind
+    a thin-layer face h = 10, three seeded delaminations, 2e9 W/m^3 flash) at 65 x 128 x 128, 100 steps of the
+    reference.  Only the layers that left the ambient temperature are stored (the rest are checked to be
+    exactly 293 K), which keeps the fixture small."""
+    spec = W.composite_panel(seed=1, nz=64, ny=128, nx=128, nsteps=100)
+    P, S, times, res = run_reference(hs, spec, {1, 20, 100})
+    d = W.spec_to_npz_dict(spec)
+    d["times"] = np.array(times)
+    d["save_steps"] = np.array([1, 20, 100])
+    for key, T in res.items():
+        moved = np.nonzero((T != 293.0).any(axis=(1, 2)))[0]
+        nk = int(moved.max()) + 1 if moved.size else 0
+        d[key + "_top"] = np.ascontiguousarray(T[:nk])
+        d[key + "_nz"] = np.int64(T.shape[0])
+        print(key, "layers away from ambient:", nk)
+    np.savez_compressed(os.path.join(HERE, "composite_panel_128.npz"), **d)
+    print("wrote composite_panel_128")
+
+
+def unaligned_fixture(hs):
+    """What the reference's setup does with unaligned_anisotropic=True (alternatingdirection_c_pyx.pyx:511-564,
+    crank_nicolson.pyx:140-143) on a tensor aligned with the axes, an unaligned tensor and a scalar-k slab with
+    fixed voxels: the exception type and where it was raised, or the stage count if it returned."""
+    import json
+    import traceback
+    cases = {}
+    for label, k, bnd in (("aligned_tensor", [[5.0, 0, 0], [0, 4.0, 0], [0, 0, 3.0]], "conducting_anisotropic"),
+                          ("unaligned_tensor", [[5.0, 0.3, 0.0], [0.3, 5.0, 0.0], [0.0, 0.0, 5.0]],
+                           "conducting_anisotropic"),
+                          ("scalar_k", None, None)):
+        spec = W.line_grid((3, 4, 5)) if k is not None else W.mixed_small()
+        if k is not None:
+            spec["boundaries"][0] = [bnd]
+            spec["materials"][0][1] = k
+        try:
+            P, S = quiet(hs.setup, *W.setup_args(hs, spec), unaligned_anisotropic=True)
+            cases[label] = {"returned_stages": len(S)}
+        except Exception as e:
+            fr = traceback.extract_tb(e.__traceback__)[-1]
+            cases[label] = {"raised": type(e).__name__, "file": os.path.basename(fr.filename), "line": fr.lineno}
+    with open(os.path.join(HERE, "unaligned_anisotropic.json"), "w") as fh:
+        json.dump(cases, fh, indent=1, sort_keys=True)
+    print("wrote unaligned_anisotropic", cases)
+
+
 def main():
     if not build_ref.available():
         build_ref.build()
     hs = build_ref.import_reference()
     if len(sys.argv) > 1 and sys.argv[1] == "curved":
         curved_fixtures(hs)
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "unaligned":
+        unaligned_fixture(hs)
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "composite128":
+        composite_panel_128(hs)
         return
     if len(sys.argv) > 1 and sys.argv[1] == "surface":
         surface_fixture(hs)
@@ -133,6 +185,8 @@ def main():
         save_fixture("line_%dx%dx%d" % shape, W.line_grid(shape), set(range(1, 6)), hs)
     curved_fixtures(hs)
     surface_fixture(hs)
+    composite_panel_128(hs)
+    unaligned_fixture(hs)
 
 
 if __name__ == "__main__":

@@ -202,33 +202,61 @@ def _fd_errors(p, dt, ckpt, voxels, h_rel=5e-2, floor=1e-3):
             r1 = [(4 * d[i + 1] - d[i]) / 3 for i in range(2)]
             fd = (16 * r1[1] - r1[0]) / 15
         g = grads[name][idx]
-        errs[(name, idx)] = abs(fd - g) / max(abs(g), floor * gmax[name])
+        floored = abs(g) < floor * gmax[name]
+        errs[(name, idx)] = (abs(fd - g) / max(abs(g), floor * gmax[name]), floored)
     return errs
+
+
+def _check_fd(errs, tol=1e-6, label=""):
+    """Every entry within tol: relative to the entry itself where it lies above the floor, relative to the floor
+    where it lies below.  Reports how many entries of each field the floor decided; returns those counts."""
+    floored = {}
+    for (name, _), (_, f) in errs.items():
+        floored[name] = floored.get(name, 0) + int(f)
+    total = {}
+    for (name, _) in errs:
+        total[name] = total.get(name, 0) + 1
+    rel = {key: e for key, (e, f) in errs.items() if not f}
+    flo = {key: e for key, (e, f) in errs.items() if f}
+    print("%s FD check: floor decided %s of %s entries; largest relative error above the floor %.2e, largest "
+          "floor-relative error below it %.2e" % (label, floored, total, max(rel.values(), default=0.0),
+                                                  max(flo.values(), default=0.0)))
+    worst = sorted(errs.items(), key=lambda kv: -kv[1][0])[:4]
+    assert max(rel.values(), default=0.0) <= tol, worst
+    assert max(flo.values(), default=0.0) <= tol, worst
+    return floored, total
 
 
 def test_gradients_match_central_differences(cuda_ok):
     """Central differences of the GPU loss at random voxels agree with the adjoint to 1e-6 relative (floored
-    at 1e-3 of the field's largest gradient)."""
+    at 1e-3 of the field's largest gradient; the number of entries the floor decided is reported and bounded)."""
     dt, N = 0.01, 80
     p = _flash_problem(4, (10, 24, 20), N)
     rng = np.random.default_rng(6)
     vox = [tuple(int(rng.integers(0, n)) for n in p["shape"]) for _ in range(12)]
     errs = _fd_errors(p, dt, 16, vox)
-    assert max(errs.values()) <= 1e-6, sorted(errs.items(), key=lambda kv: -kv[1])[:4]
+    floored, total = _check_fd(errs, label="flash (10,24,20)")
+    # a shallow grid: the surface sees every voxel, so the relative criterion decides most entries
+    assert sum(floored.values()) <= sum(total.values()) // 4, floored
 
 
 @pytest.mark.slow
 def test_steel_adjoint_central_differences_64_voxels(cuda_ok):
     """The (32,128,128) steel inverse problem, 500 steps of 10 ms, checkpoint every 50: k, rho*c and q
     gradients at 64 random voxels agree with central differences to 1e-6 relative (floored at 1e-3 of the
-    field's largest gradient)."""
+    field's largest gradient).  Entries above the floor are judged by their own relative error; how many the
+    floor decided is printed and bounded."""
     w = W.adjoint_steel()
     p = dict(k=w["k"], C=w["C"], q=w["q"], T0=w["T0"], schedule=w["schedule"], obs=w["obs"],
              spacing=w["spacing"], shape=w["shape"])
     rng = np.random.default_rng(8)
     vox = [tuple(int(rng.integers(0, n)) for n in w["shape"]) for _ in range(64)]
     errs = _fd_errors(p, w["dt"], w["ckpt"], vox)
-    assert max(errs.values()) <= 1e-6, sorted(errs.items(), key=lambda kv: -kv[1])[:4]
+    floored, total = _check_fd(errs, label="steel (32,128,128)")
+    # the floor decides only voxels the surface barely sees; at least half of each field's entries are judged by
+    # their own relative error
+    for name in total:
+        assert floored[name] <= total[name] // 2, floored
 
 
 def test_autograd_function_single(cuda_ok):

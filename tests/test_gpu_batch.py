@@ -5,6 +5,8 @@ import numpy as np
 import pytest
 
 from conftest import rel_err
+import oracle
+from oracle_shim import HS
 import heatsim2_gb300 as hs
 from heatsim2_gb300 import workloads as W
 from heatsim2_gb300.batch import Batch
@@ -75,3 +77,33 @@ def test_batch_fp32_error_against_fp64(cuda_ok):
     worst = max(rel_err(b, a) for a, b in zip(f64, f32))
     # float state as offsets from the initial mean: relative error ~1e-8 of max|T| (1e-6 without the offset)
     assert worst < 1e-7, worst
+
+
+def _oracle(spec, nsteps):
+    Po, _ = oracle.setup(*W.setup_args(HS, spec))
+    vol = W.volumetric_tuple(HS, spec)
+    T = W.initial_temperature(spec)
+    for t in W.step_times(spec, nsteps):
+        T = oracle.run_adi_steps(Po, None, t, spec["dt"], T, spec["arrays"]["volumetric"], vol)
+    return T
+
+
+def test_benchmark_batch_instances_vs_oracle(cuda_ok):
+    """The first 8 instances of the 256-instance benchmark batch (seed 2: nz 16..64, ny and nx 64..256, odd
+    row widths among them, steel and composite), 10 steps in one batched state.  Each instance is compared
+    with the oracle: FP64 within 1e-12 of max|T|, the FP32 variant within 1e-7 (its stated error is ~1e-8)."""
+    nsteps = 10
+    specs = W.uneven_batch(seed=2, n=8, nsteps=nsteps)
+    assert sum(s["grid"]["nx"] % 2 for s in specs) >= 3
+    assert max(s["grid"]["ny"] for s in specs) >= 200
+    f64 = _batch(specs, nsteps)
+    f32 = _batch(specs, nsteps, precision=32)
+    worst64 = worst32 = 0.0
+    for spec, a, b in zip(specs, f64, f32):
+        ref = _oracle(spec, nsteps)
+        assert np.abs(ref - 293.0).max() > 1.0            # the flash reached the field
+        worst64 = max(worst64, rel_err(a, ref))
+        worst32 = max(worst32, rel_err(b, ref))
+    print("batch vs oracle: FP64 %.2e, FP32 %.2e" % (worst64, worst32))
+    assert worst64 <= 1e-12, worst64
+    assert worst32 <= 1e-7, worst32

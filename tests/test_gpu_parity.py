@@ -158,9 +158,62 @@ def test_uneven_instances_vs_oracle(cuda_ok):
 
 
 def test_full_size_composite_panel_first_steps_vs_oracle(cuda_ok):
-    """The benchmark workload itself (65x512x512 with the ambient layer), two steps against the oracle."""
+    """The benchmark workload itself (65x512x512 with the ambient layer), the bench's timed step count (20
+    steps, the flash included) against the oracle, every step."""
     spec = W.composite_panel(seed=1)
-    _compare_with_oracle(spec, 2)
+    _compare_with_oracle(spec, 20)
+
+
+def test_composite_panel_128_device_run_vs_reference(cuda_ok):
+    """The benchmark's composite-panel recipe at 65x128x128 (reference-generated fixture, 100 steps): the
+    device-resident multi-step path (hs.run on a CUDA tensor) at steps 1, 20 and 100."""
+    import torch
+    spec, times, ref = load_golden(GOLDEN + "/composite_panel_128.npz")
+    assert sorted(ref) == [1, 20, 100]
+    P, S = _setup(spec)
+    vol = W.volumetric_tuple(hs, spec)
+    T = torch.from_numpy(W.initial_temperature(spec)).cuda()
+    done = 0
+    for n in (1, 20, 100):
+        T = hs.run(P, T, times[done:n], spec["dt"], spec["arrays"]["volumetric"], vol)
+        done = n
+        assert rel_err(T.cpu().numpy(), ref[n]) <= TOL, (n, rel_err(T.cpu().numpy(), ref[n]))
+
+
+def _class_sources(spec, P, t):
+    from heatsim2_gb300.alternatingdirection import _ClassSources, source_table
+    q, _ = source_table(_ClassSources(W.volumetric_tuple(hs, spec)), t, spec["dt"], P.volume_array)
+    return q
+
+
+@pytest.mark.parametrize("name", ["mixed_small", "steel_slab"])
+def test_dense_handle_from_compiled_faces_vs_reference(cuda_ok, name):
+    """hs2g_create_dense fed the compiled face conductances, capacities and fixed mask of a reference fixture
+    (P.faces()) reproduces the reference's temperatures: the dense entry point is pinned to the reference, not
+    only to the class-compiled path."""
+    import ctypes
+    from heatsim2_gb300 import _native
+    spec, times, ref = load_golden(GOLDEN + "/%s.npz" % name)
+    P, S = _setup(spec)
+    Gz, Gy, Gx, M, fixed = P.faces()
+    vclass = np.ascontiguousarray(spec["arrays"]["volumetric"], dtype=np.uint8)
+    nz, ny, nx = P.shape
+    L = _native.load()
+    dense = _native.DenseProblem(nz, ny, nx, Gz.ctypes.data, Gy.ctypes.data, Gx.ctypes.data, M.ctypes.data,
+                                 fixed.ctypes.data, vclass.ctypes.data)
+    h = ctypes.c_void_p()
+    _native.check(L.hs2g_create_dense(ctypes.byref(dense), P.device, ctypes.byref(h)))
+    try:
+        T = W.initial_temperature(spec)
+        for n, t in enumerate(times):
+            q = _class_sources(spec, P, t)
+            out = np.empty_like(T)
+            _native.check(L.hs2g_step(h, T.ctypes.data, out.ctypes.data, q.ctypes.data, None, None, 0))
+            T = out
+            if n + 1 in ref:
+                assert rel_err(T, ref[n + 1]) <= TOL, (n + 1, rel_err(T, ref[n + 1]))
+    finally:
+        L.hs2g_destroy(h)
 
 
 def test_full_size_energy_conservation(cuda_ok):

@@ -1,18 +1,23 @@
-"""hs2g_step_static, the timestep entry point that allocates no device memory, against hs2g_step.
+"""hs2g_step_static, the timestep entry point that allocates no device memory, against hs2g_step and against
+the reference's own outputs.
 
 hs2g_step_static is for callers that cannot allocate device memory themselves -- a plugin whose host
 application owns every device allocation.  It takes the problem (face conductances, capacities, fixed mask,
 source) in caller-owned device memory and keeps its intermediates in a static device array, so it must give the
 same timestep as a compiled handle (hs2g_create_dense + hs2g_step) on the same inputs.  The tensors below are
 allocated by the test, not by the entry point.  Tolerance: 1e-12 relative max error, as for every GPU parity
-test.  Two calls in a row check that the shared array's leftover contents do not leak into the next call.
+test.  Two calls in a row check that the shared array's leftover contents do not leak into the next call; the
+reference fixtures (tests/golden) pin the entry point to the reference itself over whole runs.
 """
 import ctypes
 
 import numpy as np
 import pytest
 
+from conftest import GOLDEN, load_golden, rel_err
+import heatsim2_gb300 as hs
 from heatsim2_gb300 import _native
+from heatsim2_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12
@@ -77,3 +82,73 @@ def test_static_step_rejects_grids_beyond_the_maximum(cuda_ok):
     rc = L.hs2g_step_static(nz, ny, nx, dummy, dummy, dummy, dummy, None, None, dummy, dummy, None)
     assert rc == _native.ERR_ARG
     assert b"HS2G_STATIC_MAX_VOXELS" in L.hs2g_last_error()
+
+
+def _source_field(spec, P, t):
+    """The per-voxel source (W/m^3) of a fixture at time t: class-uniform values scattered by the class map,
+    plus the per-voxel kinds."""
+    from heatsim2_gb300.alternatingdirection import _ClassSources, _dense_source, source_table
+    vol = W.volumetric_tuple(hs, spec)
+    src = _ClassSources(vol)
+    q, _ = source_table(src, t, spec["dt"], P.volume_array)
+    vclass = np.asarray(spec["arrays"]["volumetric"])
+    Q = q[vclass]
+    if src.dense:
+        qd = _dense_source(P.shape, P.volume_array, t, spec["dt"], vclass, src.dense)
+        if qd is not None:
+            Q = Q + qd
+    return np.ascontiguousarray(Q)
+
+
+@pytest.mark.parametrize("name", ["mixed_small", "sources_small", "steel_slab"])
+def test_static_step_vs_reference_fixture(cuda_ok, name):
+    """hs2g_step_static fed a reference fixture's compiled faces (P.faces()) and its sources as a per-voxel
+    field reproduces the reference's temperatures within 1e-12: the no-allocation step is pinned to the
+    reference itself (fixed voxels, every source kind and the 200-step steel slab)."""
+    import torch
+    L = _native.load()
+    spec, times, ref = load_golden(GOLDEN + "/%s.npz" % name)
+    P, _ = hs.setup(*W.setup_args(hs, spec))
+    Gz, Gy, Gx, M, fixed = P.faces()
+    nz, ny, nx = P.shape
+    dev = torch.device("cuda", P.device)
+    g = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+         for k, v in dict(Gz=Gz, Gy=Gy, Gx=Gx, M=M, fixed=fixed).items()}
+    stream = torch.cuda.current_stream(dev)
+    T = torch.from_numpy(W.initial_temperature(spec)).to(dev)
+    out = torch.empty_like(T)
+    for n, t in enumerate(times):
+        Q = torch.from_numpy(_source_field(spec, P, t)).to(dev)
+        _native.check(L.hs2g_step_static(nz, ny, nx, g["Gz"].data_ptr(), g["Gy"].data_ptr(), g["Gx"].data_ptr(),
+                                         g["M"].data_ptr(), g["fixed"].data_ptr(), Q.data_ptr(), T.data_ptr(),
+                                         out.data_ptr(), ctypes.c_void_p(stream.cuda_stream)))
+        T, out = out, T
+        if n + 1 in ref:
+            err = rel_err(T.cpu().numpy(), ref[n + 1])
+            assert err <= TOL, (n + 1, err)
+
+
+def test_static_step_rejects_bad_capacity(cuda_ok):
+    """A computed voxel with a non-positive capacity is reported (HS2G_ERR_CAPACITY, with its index), and the
+    next call with valid inputs succeeds: the status word is cleared per call."""
+    import torch
+    L = _native.load()
+    Gz, Gy, Gx, M, fixed, Q, T = _problem(7, nz=4, ny=5, nx=6)
+    fixed[:] = 0
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream()
+    bad_values = ((0.0, _native.ERR_CAPACITY), (-3.0, _native.ERR_CAPACITY), (float("nan"), _native.ERR_CAPACITY),
+                  (None, _native.OK))
+    for bad, expect in bad_values:
+        Mb = M.copy()
+        if bad is not None:
+            Mb[2, 3, 4] = bad
+        d = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+             for k, v in dict(Gz=Gz, Gy=Gy, Gx=Gx, M=Mb, fixed=fixed, T=T).items()}
+        out = torch.empty_like(d["T"])
+        rc = L.hs2g_step_static(4, 5, 6, d["Gz"].data_ptr(), d["Gy"].data_ptr(), d["Gx"].data_ptr(),
+                                d["M"].data_ptr(), d["fixed"].data_ptr(), None, d["T"].data_ptr(),
+                                out.data_ptr(), ctypes.c_void_p(stream.cuda_stream))
+        assert rc == expect, (bad, rc, L.hs2g_last_error())
+        if bad is not None:
+            assert b"[2,3,4]" in L.hs2g_last_error()
