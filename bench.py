@@ -12,9 +12,11 @@ throw-away copy.  Synthetic, seeded input (heatsim2_gb300.workloads.composite_pa
 Prints one JSON line.  ``value`` counts computed voxels (64*512*512) per second with the state resident in
 HBM; ``e2e`` is the same metric through the C ABI with host buffers (host->device copy of T, the step,
 device->host copy of T, every step); ``roofline`` is the dominant sweep kernel against the measured HBM copy
-bandwidth; ``step_hbm`` the whole step against it (this implementation's bytes, and the 136-byte accounting
-of a step that re-reads T, M and the face conductances in every sweep); ``fp64_roofline`` the whole step
-against the measured FP64 FMA rate, the resource that binds;
+bandwidth, on the algorithmic bytes of a sweep that reads each array it needs once with the face conductances
+and capacities re-read in every sweep (x 56, y 40, z 40 B per voxel: 136 B per step), with this
+implementation's own bytes (x 88 B: T, nine step coefficients, W0) and the ncu-measured DRAM traffic beside
+it; ``kernel_hbm_frac`` gives the same for every sweep; ``step_hbm`` the whole step against the bandwidth
+(both accountings); ``fp64_roofline`` the whole step against the measured FP64 FMA rate;
 ``cpu_baseline`` the reference (or, where it cannot be built, the oracle) on the host cores.  ``batched`` is
 the 256-instance uneven batch (FP64 and FP32) against a per-instance loop of the plain path; ``adjoint`` the
 gradient evaluations per second of the (32,128,128) steel inverse problem and of the 32-instance batched
@@ -41,6 +43,12 @@ SEED = 1
 #   sweep_y  reads W0, a1, b1, writes W1
 #   sweep_z  reads W1, a2, b2, T, writes T'
 BYTES_PER_VOXEL = {"sweep_x": 8 + 9 * 8 + 8, "sweep_y": 4 * 8, "sweep_z": 5 * 8}
+# the algorithmic bytes the roofline is reported on: each sweep touching each array it needs once, with the face
+# conductances and capacities re-read in every sweep (136 B per voxel and step):
+#   sweep_x  reads T, M, Gx, Gy, Gz, Q, writes T*0 (7 arrays)
+#   sweep_y  reads T, T*0, M, Gy, writes T*1 (5)
+#   sweep_z  reads T, T*1, M, Gz, writes T' (5)
+ROOFLINE_BYTES_PER_VOXEL = {"sweep_x": 7 * 8, "sweep_y": 5 * 8, "sweep_z": 5 * 8}
 FP64_OPS_PER_VOXEL = {"sweep_x": 9, "sweep_y": 2, "sweep_z": 3}
 KERNELS = ("sweep_x", "sweep_y", "sweep_z")
 # adjoint: arrays touched per voxel and step (8 B each), from the kernels of hs2g_adjoint.cu
@@ -548,12 +556,16 @@ def gpu_arm(args, world, rank, local_rank):
     # roofline of the dominant kernel
     hbm_peak, peak_src = read_peaks()
     dom = max(per_kernel_ms, key=per_kernel_ms.get)
-    achieved_gbs = BYTES_PER_VOXEL[dom] * grid_vox / (per_kernel_ms[dom] * 1e-3) / 1e9
+    achieved_gbs = ROOFLINE_BYTES_PER_VOXEL[dom] * grid_vox / (per_kernel_ms[dom] * 1e-3) / 1e9
+    impl_gbs = BYTES_PER_VOXEL[dom] * grid_vox / (per_kernel_ms[dom] * 1e-3) / 1e9
     traffic = read_traffic()
     roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved_gbs / hbm_peak, "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
-                "algorithmic_bytes_per_launch": BYTES_PER_VOXEL[dom] * grid_vox,
-                "traffic": traffic[dom] * grid_vox if dom in traffic else None}
+                "algorithmic_bytes_per_voxel": ROOFLINE_BYTES_PER_VOXEL[dom],
+                "algorithmic_bytes_per_launch": ROOFLINE_BYTES_PER_VOXEL[dom] * grid_vox,
+                "traffic": traffic[dom] * grid_vox if dom in traffic else None,
+                "implementation_bytes_per_voxel": BYTES_PER_VOXEL[dom], "implementation_achieved": impl_gbs,
+                "implementation_frac": impl_gbs / hbm_peak}
     step_ops = sum(FP64_OPS_PER_VOXEL.values()) * grid_vox
     fp64 = {"bound": "fp64", "achieved": step_ops / (total_ms * 1e-3 / K) / 1e12,
             "peak": fma_rate.value / 1e12, "unit": "TFMA/s", "ops_per_voxel_step": sum(FP64_OPS_PER_VOXEL.values()),
@@ -568,8 +580,12 @@ def gpu_arm(args, world, rank, local_rank):
                 "achieved_gbs": sum(BYTES_PER_VOXEL.values()) * grid_vox / step_s / 1e9,
                 "frac": sum(BYTES_PER_VOXEL.values()) * grid_vox / step_s / 1e9 / hbm_peak,
                 "frac_136_bytes": 136 * compute_vox / step_s / 1e9 / hbm_peak, "peak": hbm_peak}
-    per_kernel_hbm = {k: BYTES_PER_VOXEL[k] * grid_vox / (per_kernel_ms[k] * 1e-3) / 1e9 / hbm_peak
+    per_kernel_hbm = {k: ROOFLINE_BYTES_PER_VOXEL[k] * grid_vox / (per_kernel_ms[k] * 1e-3) / 1e9 / hbm_peak
                       for k in KERNELS}
+    per_kernel_hbm_impl = {k: BYTES_PER_VOXEL[k] * grid_vox / (per_kernel_ms[k] * 1e-3) / 1e9 / hbm_peak
+                           for k in KERNELS}
+    per_kernel_traffic = {k: traffic[k] * grid_vox / (per_kernel_ms[k] * 1e-3) / 1e9 / hbm_peak
+                          for k in KERNELS if k in traffic}
     # end to end through the C ABI with pinned host buffers
     e2e = None
     if not args.no_e2e:
@@ -622,7 +638,8 @@ def gpu_arm(args, world, rank, local_rank):
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": roofline, "fp64_roofline": fp64, "step_hbm": step_hbm,
             "kernel_ms_per_step": per_kernel_ms, "kernel_fp64_frac": per_kernel_fp64,
-            "kernel_hbm_frac": per_kernel_hbm,
+            "kernel_hbm_frac": per_kernel_hbm, "kernel_hbm_frac_implementation_bytes": per_kernel_hbm_impl,
+            "kernel_dram_frac_measured_traffic": per_kernel_traffic,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * K, "clocks": clk, "setup_s": setup_s,
             "device_bytes": state_bytes, "batched": batched, "adjoint": adjoint, "curved": curved,
         }

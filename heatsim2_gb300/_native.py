@@ -17,7 +17,8 @@ OK = 0
 ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_EXTERIOR, ERR_KTYPE, ERR_UNALIGNED, ERR_FORM, ERR_CAPACITY, ERR_STATE = \
     -1, -2, -3, -4, -5, -6, -7, -8, -9
 ERR_TIMEOUT = -10
-DEVICE, SYNC = 1, 2
+DEVICE, SYNC, REUSE = 1, 2, 4
+SHAPED_IMPULSE = 5
 K_ENTRIES = 10
 FORM_LEN = 1 + 2 * K_ENTRIES
 MAX_ZERO_FORMS = 24
@@ -32,7 +33,8 @@ EXPORTED = ("hs2g_abi_version", "hs2g_last_error", "hs2g_create_classes", "hs2g_
             "hs2g_adjoint_create", "hs2g_adjoint_destroy", "hs2g_adjoint_set_stream", "hs2g_adjoint_layout",
             "hs2g_adjoint_device_bytes", "hs2g_adjoint_set_parameters", "hs2g_adjoint_forward",
             "hs2g_adjoint_backward", "hs2g_create_rows", "hs2g_selftest_wait", "hs2g_run_surface",
-            "hs2g_surface_temperature")
+            "hs2g_surface_temperature", "hs2g_set_source_classes", "hs2g_source_zdecay", "hs2g_source_point",
+            "hs2g_adjoint_set_faces")
 STATIC_MAX_VOXELS = 1 << 20
 
 
@@ -130,6 +132,14 @@ def load():
         L.hs2g_surface_temperature.restype = i32
         L.hs2g_source_table.argtypes = [i32, vp, vp, dp, dp, dp, vp]
         L.hs2g_source_table.restype = i32
+        L.hs2g_set_source_classes.argtypes = [vp, vp, i32]
+        L.hs2g_set_source_classes.restype = i32
+        L.hs2g_source_zdecay.argtypes = [vp, i32, vp, dp, dp, dp, dp, dp, dp, i32]
+        L.hs2g_source_zdecay.restype = i32
+        L.hs2g_source_point.argtypes = [vp, i32, vp, i64, vp, dp, dp, i32]
+        L.hs2g_source_point.restype = i32
+        L.hs2g_adjoint_set_faces.argtypes = [vp, i32, vp, vp, vp, vp, vp, i32]
+        L.hs2g_adjoint_set_faces.restype = i32
         L.hs2g_get_faces.argtypes = [vp, vp, vp, vp, vp, vp]
         L.hs2g_get_faces.restype = i32
         L.hs2g_run_timed.argtypes = [vp, i32, vp, vp, vp, i32, vp]

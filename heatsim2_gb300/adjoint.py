@@ -1,9 +1,11 @@
 """Gradients of a surface-temperature misfit through the ADI step (libhs2g hs2g_adjoint_*).
 
 No counterpart in the reference, which has no derivatives.  The model is the per-voxel form of the
-reference's step: a fully computed box with per-voxel conductivity k (W/m/K), volumetric heat capacity
-C = rho*c (J/m^3/K) and source amplitude q (W/m^3, scaled per step by a schedule), insulating outside and
-conducting inside with the arithmetic face mean of boundary_conducting.py:7-71.  The loss of an instance is
+reference's step: a box with per-voxel conductivity k (W/m/K), volumetric heat capacity C = rho*c (J/m^3/K)
+and source amplitude q (W/m^3, scaled per step by a schedule), insulating outside and conducting inside with
+the arithmetic face mean of boundary_conducting.py:7-71, or (``Adjoint.set_faces``) with the face classes of
+a class problem -- conducting, insulating, thin insulating layers, any class affine in a scalar k -- and
+fixed-temperature voxels.  The loss of an instance is
     J = sum_n sum_{y,x} (T_{n+1}[0, y, x] - obs[n, y, x])^2
 (layer 0 is the heated surface).  The forward pass checkpoints T every ``ckpt`` steps; the backward pass
 recomputes one segment at a time and runs the transposed tridiagonal solves in reverse order on the GPU.
@@ -84,6 +86,53 @@ class Adjoint(object):
     def _split(self, buf):
         out = [buf[self.offsets[i]:self.offsets[i + 1]].reshape(self.grids[i][0]) for i in range(self.n)]
         return out[0] if self.n == 1 else out
+
+    def set_faces(self, faces=None, fixed=None):
+        """Face classes and fixed voxels (call before ``set_parameters``); None restores the default (every
+        interior face conducting with the arithmetic mean of k, every voxel computed).
+
+        ``faces``: per instance ``(boundaries, boundary_z_elements, boundary_y_elements, boundary_x_elements)``
+        as ``heatsim2.setup`` takes them: a tuple of boundary classes ``(module, *extra)`` and uint8 class arrays
+        of shapes (nz+1, ny, nx), (nz, ny+1, nx), (nz, ny, nx+1).  Each class is evaluated for scalar k into its
+        affine face form (``face_forms``).  ``fixed``: per instance a (nz, ny, nx) mask of fixed-temperature
+        voxels, or None.  Lists of them for a batch."""
+        L = _native.load()
+        if faces is None and fixed is None:
+            _native.check(L.hs2g_adjoint_set_faces(self._h, 0, None, None, None, None, None, 0))
+            return
+        if faces is None:
+            faces = [None] * self.n
+        elif self.n == 1 and not isinstance(faces, list):
+            faces = [faces]
+        if fixed is not None and self.n == 1 and not isinstance(fixed, list):
+            fixed = [fixed]
+        if len(faces) != self.n or (fixed is not None and len(fixed) != self.n):
+            raise ValueError("faces / fixed: one entry per instance")
+        per = []
+        for i, spec in enumerate(faces):
+            shape, spacing = self.grids[i]
+            fx_i = None if fixed is None or fixed[i] is None else np.asarray(fixed[i]).astype(bool)
+            if fx_i is not None and fx_i.shape != shape:
+                raise ValueError("fixed of instance %d: shape %s, expected %s" % (i, fx_i.shape, shape))
+            per.append(face_classes(shape, spacing, spec, fx_i))
+        nclass = max(f.shape[0] for f, _ in per)
+        forms = np.zeros((self.n, nclass, 3, 3))
+        for i, (f, _) in enumerate(per):
+            forms[i, :f.shape[0]] = f
+        cls = [np.empty(self.voxels, dtype=np.uint8) for _ in range(3)]
+        for i, (_, low) in enumerate(per):
+            for a in range(3):
+                cls[a][self.offsets[i]:self.offsets[i + 1]] = low[a].reshape(-1)
+        fixed_buf = None
+        if fixed is not None:
+            fixed_buf = np.zeros(self.voxels, dtype=np.uint8)
+            for i, m in enumerate(fixed):
+                if m is not None:
+                    fixed_buf[self.offsets[i]:self.offsets[i + 1]] = np.asarray(m).astype(bool).reshape(-1)
+        forms = np.ascontiguousarray(forms)
+        _native.check(L.hs2g_adjoint_set_faces(self._h, nclass, forms.ctypes.data, cls[0].ctypes.data,
+                                               cls[1].ctypes.data, cls[2].ctypes.data,
+                                               None if fixed_buf is None else fixed_buf.ctypes.data, 0))
 
     def set_parameters(self, k, C, q):
         """Per-voxel k, C = rho*c and q: one (nz, ny, nx) array each, or lists of them for a batch."""
@@ -173,6 +222,69 @@ class Adjoint(object):
         self.backward_ms = ms.value
 
 
+def face_forms(boundaries, spacing):
+    """[nclass][3][3] affine scalar-k face forms (f0, flo, fhi) per class and axis (z, y, x): the conductance
+    G = f0 + flo k_lo + fhi k_hi (W/m^3/K) each boundary class gives a face, from the same symbolic evaluation
+    as ``setup`` (heatsim2_gb300.crank_nicolson.compile_boundary_forms).  Classes that use a conductivity
+    tensor, or whose flux is not a two-point difference for every scalar k, raise ValueError."""
+    from .crank_nicolson import compile_boundary_forms
+    dz, dy, dx = spacing
+    ff = compile_boundary_forms(boundaries, dz, dy, dx)
+    K = _native.K_ENTRIES
+    out = np.zeros((len(boundaries), 3, 3))
+    for b in range(len(boundaries)):
+        for a in range(3):
+            f = ff[3 * b + a]
+            normal = np.array(f.normal[:])
+            if np.any(normal[2:1 + K]) or np.any(normal[2 + K:]):
+                raise ValueError("boundary class %d: the adjoint takes a scalar k per voxel, this class uses the "
+                                 "conductivity tensor" % b)
+            for z in range(f.nzero):
+                zf = np.array(f.zero[z][:])
+                if zf[0] or zf[1] or zf[1 + K]:
+                    raise ValueError("boundary class %d: its flux is not a two-point difference for scalar k "
+                                     "(error %d)" % (b, f.zero_code[z]))
+            out[b, a] = (normal[0], normal[1], normal[1 + K])
+    return out
+
+
+def face_classes(shape, spacing, spec, fixed=None):
+    """(forms, (low_z, low_y, low_x)) of one instance: the class forms and each voxel's low-face class per axis.
+    spec None: every interior face conducting (boundary_conducting's form).  Exterior faces next to a computed
+    voxel must conduct nothing, as in the reference (alternatingdirection_c.c:158-163)."""
+    nz, ny, nx = shape
+    if spec is None:
+        dz, dy, dx = spacing
+        forms = np.zeros((1, 3, 3))
+        for a, d in enumerate((dz, dy, dx)):
+            forms[0, a] = (0.0, 0.5 / (d * d), 0.5 / (d * d))
+        zeros = np.zeros(shape, dtype=np.uint8)
+        return forms, (zeros, zeros, zeros)
+    boundaries, bz, by, bx = spec
+    forms = face_forms(boundaries, spacing)
+    arrs = []
+    for name, arr, want in (("boundary_z_elements", bz, (nz + 1, ny, nx)), ("boundary_y_elements", by, (nz, ny + 1, nx)),
+                            ("boundary_x_elements", bx, (nz, ny, nx + 1))):
+        arr = np.asarray(arr)
+        if arr.dtype != np.uint8 or arr.shape != want:
+            raise ValueError("%s must be a uint8 array of shape %s" % (name, want))
+        if int(arr.max(initial=0)) >= len(boundaries):
+            raise ValueError("%s holds a class past the boundaries tuple" % name)
+        arrs.append(arr)
+    bz, by, bx = arrs
+    comp = np.ones(shape, dtype=bool) if fixed is None else ~np.asarray(fixed, dtype=bool)
+    conducts = np.any(forms != 0.0, axis=2)     # [class][axis]
+    # each exterior face class with the voxels beside it: low and high side of z, y, x
+    exterior = ((0, bz[0], comp[0]), (0, bz[nz], comp[-1]), (1, by[:, 0], comp[:, 0]), (1, by[:, ny], comp[:, -1]),
+                (2, bx[..., 0], comp[..., 0]), (2, bx[..., nx], comp[..., -1]))
+    for a, outer, beside in exterior:
+        if np.any(conducts[outer, a] & beside):
+            raise ValueError("a computed voxel has a conducting exterior face (axis %d); the reference requires "
+                             "exterior faces to be insulating" % a)
+    low = (np.ascontiguousarray(bz[:nz]), np.ascontiguousarray(by[:, :ny]), np.ascontiguousarray(bx[:, :, :nx]))
+    return forms, low
+
+
 # handles idle between a forward and its backward are not shared; finished ones are reused per layout
 _pool = {}
 _pool_lock = threading.Lock()
@@ -198,7 +310,7 @@ def _autograd_function():
         """Flat concatenated k, C, q, T0 (float64, CUDA), obs concatenated per instance -> loss per instance."""
 
         @staticmethod
-        def forward(ctx, k, C, q, T0, obs, grids, schedule, dt, ckpt):
+        def forward(ctx, k, C, q, T0, obs, grids, schedule, dt, ckpt, faces=None, fixed=None):
             for name, t in (("k", k), ("C", C), ("q", q), ("T0", T0), ("obs", obs)):
                 if not t.is_cuda or t.dtype != torch.float64:
                     raise TypeError("%s must be a CUDA float64 tensor" % name)
@@ -217,6 +329,7 @@ def _autograd_function():
                 shift = T0.detach().mean()
                 T0s = (T0.detach() - shift).contiguous()
                 obss = (obs.detach() - shift).contiguous()
+                a.set_faces(faces, fixed)          # pooled handles: the faces of this call, or the default
                 a.set_parameters_device(k, C, q)
                 loss = a.forward_device(T0s, obss, schedule, ckpt)
             ctx.adj, ctx.key = a, key
@@ -238,7 +351,7 @@ def _autograd_function():
             scale = torch.repeat_interleave(grad_loss.to(torch.float64),
                                             torch.tensor(np.diff(a.offsets), device=dev))
             gk, gC, gq, gT0 = (t * scale for t in g)
-            return gk, gC, gq, gT0, None, None, None, None, None
+            return gk, gC, gq, gT0, None, None, None, None, None, None, None
 
     return _BatchMisfit
 
@@ -253,10 +366,11 @@ def _function():
     return _fn
 
 
-def batch_surface_misfit(k, C, q, T0, obs, schedule, spacing, dt, ckpt=50):
+def batch_surface_misfit(k, C, q, T0, obs, schedule, spacing, dt, ckpt=50, faces=None, fixed=None):
     """Losses (tensor of n) of n instances; k, C, q, T0 lists of (nz_i, ny_i, nx_i) CUDA float64 tensors, obs a
     list of (nsteps, ny_i, nx_i) tensors, spacing one (dz, dy, dx) or a list of them.  Differentiable with
-    respect to k, C, q and T0.  Temperatures are shifted by the mean of all T0 on the device."""
+    respect to k, C, q and T0.  Temperatures are shifted by the mean of all T0 on the device.  faces / fixed:
+    per instance, face classes and fixed voxels as ``Adjoint.set_faces`` takes them (lists, or None)."""
     import torch
     n = len(k)
     spacing = list(spacing) if isinstance(spacing[0], (list, tuple)) else [tuple(spacing)] * n
@@ -264,10 +378,12 @@ def batch_surface_misfit(k, C, q, T0, obs, schedule, spacing, dt, ckpt=50):
     flat = [torch.cat([t.reshape(-1) for t in arr]) for arr in (k, C, q, T0)]
     ob = torch.cat([o.reshape(-1) for o in obs])
     sched = tuple(float(v) for v in np.asarray(schedule, dtype="d").reshape(-1))
-    return _function().apply(flat[0], flat[1], flat[2], flat[3], ob, grids, sched, float(dt), int(ckpt))
+    return _function().apply(flat[0], flat[1], flat[2], flat[3], ob, grids, sched, float(dt), int(ckpt), faces,
+                             fixed)
 
 
-def surface_misfit(k, C, q, T0, obs, schedule, spacing, dt, ckpt=50):
+def surface_misfit(k, C, q, T0, obs, schedule, spacing, dt, ckpt=50, faces=None, fixed=None):
     """Loss (0-d tensor) of one instance: k, C, q, T0 (nz, ny, nx) and obs (nsteps, ny, nx) CUDA float64
-    tensors.  Differentiable with respect to k, C, q and T0."""
-    return batch_surface_misfit([k], [C], [q], [T0], [obs], schedule, spacing, dt, ckpt)[0]
+    tensors.  Differentiable with respect to k, C, q and T0.  faces / fixed as ``Adjoint.set_faces``."""
+    return batch_surface_misfit([k], [C], [q], [T0], [obs], schedule, spacing, dt, ckpt,
+                                None if faces is None else [faces], None if fixed is None else [fixed])[0]

@@ -85,7 +85,10 @@ class adi_step(object):
 # sources
 # --------------------------------------------------------------------------------------------------------
 class _ClassSources(object):
-    """The class-uniform sources of a ``volumetric`` tuple, packed for hs2g_source_table."""
+    """The sources of a ``volumetric`` tuple, packed for hs2g_source_table.  Class-uniform kinds are evaluated
+    per class; the kinds whose value differs between a class's voxels (point joules with per-voxel values or
+    per-cell volumes, the z-decaying impulse) become HS2G_SHAPED_IMPULSE classes whose per-voxel values the
+    device evaluates into the handle's source shape (``_prepare_shapes``)."""
 
     def __init__(self, volumetric, per_voxel_volume=False):
         """per_voxel_volume: the problem's cells differ in volume (curved-surface mode), so point-joules sources
@@ -95,7 +98,7 @@ class _ClassSources(object):
             raise ValueError("at most 256 source classes")
         self.kind = np.zeros(max(n, 1), dtype=np.int32)
         self.params = np.zeros((max(n, 1), 4))
-        self.dense = []                     # (class index, source tuple) evaluated per voxel on the host
+        self.shaped = []                    # (class index, source tuple) evaluated per voxel on the device
         for c, src in enumerate(volumetric):
             k = src[0]
             if k in (NO_SOURCE, IMPULSE_SOURCE, STEPPED_SOURCE):
@@ -107,55 +110,85 @@ class _ClassSources(object):
                     self.kind[c] = k
                     self.params[c, :2] = (float(src[1]), float(src[2]))
                 else:
-                    self.kind[c] = NO_SOURCE
-                    self.dense.append((c, src))
+                    self.kind[c] = _native.SHAPED_IMPULSE
+                    self.params[c, 0] = float(src[1])
+                    self.shaped.append((c, src))
             elif k == SPATIALLY_Z_DECAYING_TEMPORAL_IMPULSE:
-                self.kind[c] = NO_SOURCE
-                self.dense.append((c, src))
+                self.kind[c] = _native.SHAPED_IMPULSE
+                self.params[c, 0] = float(src[1])
+                self.shaped.append((c, src))
             else:
                 raise ValueError("unknown volumetric source kind %r (class %d)" % (k, c))
         self.n = n
 
 
-def _dense_source(shape, volume, t, dt, volumetric_elements, dense):
-    """Per-voxel source field for the sources that are not uniform over their class (pyx:307-384), or None
-    when none of them fires at t."""
-    q = None
-    for idx, src in dense:
-        kind = src[0]
-        if kind == IMPULSE_POINT_SOURCE_JOULES:
-            if t == src[1]:
-                if q is None:
-                    q = np.zeros(shape)
-                sel = volumetric_elements == idx
-                if np.ndim(volume) > 0:     # per-cell volumes (curved-surface mode)
-                    q[sel] = src[2] / (volume[sel] * dt)
-                else:
-                    q[sel] = src[2] / (volume * dt)
-        else:
+def _same_array(P, key, a):
+    """True when ``a`` is the array last uploaded under ``key`` for this problem (same object, same memory),
+    so the device keeps its copy; records ``a`` otherwise."""
+    cache = P.__dict__.setdefault("_shape_arrays", {})
+    old = cache.get(key)
+    if old is not None and old[0] is a and old[1] == a.ctypes.data:
+        return True
+    cache[key] = (a, a.ctypes.data)
+    return False
+
+
+def _prepare_shapes(P, sources, times, dt, volumetric_elements):
+    """Evaluate on the device the source shapes of the shaped classes that fire at one of ``times``
+    (pyx:307-384).  A shape is re-evaluated when its source tuple, dt or the device's class map changed since
+    it was evaluated; its per-voxel inputs (z coordinates, per-voxel joules, cell volumes) are uploaded once
+    and kept on the device while the same arrays are passed."""
+    if not sources.shaped:
+        return
+    L = _native.load()
+    done = P.__dict__.setdefault("_shapes", {})
+    tset = set(float(t) for t in times)
+    for c, src in sources.shaped:
+        if float(src[1]) not in tset:
+            continue
+        key = (tuple(id(v) for v in src), tuple(float(v) for v in src if isinstance(v, numbers.Number)), float(dt),
+               id(P.compiled_volumetric))
+        if done.get(c) == key:
+            continue
+        if src[0] == SPATIALLY_Z_DECAYING_TEMPORAL_IMPULSE:
             (_, t_imp, direc, offset, zgrid, ddz, jpm2, length) = src
-            if t == t_imp:
-                direc = np.asarray(direc, dtype="d")
-                if not ((direc == np.array([1.0, 0.0, 0.0])).all() or (direc == np.array([-1.0, 0.0, 0.0])).all()):
-                    raise AssertionError("decay direction must be +z or -z")
-                length = float(length)
-                if not length > 0:
-                    raise AssertionError("characteristic length must be positive")
-                if q is None:
-                    q = np.zeros(shape)
-                sel = volumetric_elements == idx
-                centre = zgrid * direc[0] - float(offset)
-                ddz = abs(float(ddz))
-                left = centre - ddz / 2.0
-                right = centre + ddz / 2.0
-                use = sel & (right > 0.0)
-                r = right[use]
-                lft = left[use]
-                lft[lft < 0.0] = 0.0
-                # fraction of a (1/l) exp(-d/l) profile deposited between the cell's z boundaries
-                frac = -np.exp(-r / length) + np.exp(-lft / length)
-                q[use] = frac * float(jpm2) / (ddz * dt)
-    return q
+            direc = np.asarray(direc, dtype="d")
+            if not ((direc == np.array([1.0, 0.0, 0.0])).all() or (direc == np.array([-1.0, 0.0, 0.0])).all()):
+                raise AssertionError("decay direction must be +z or -z")
+            length = float(length)
+            if not length > 0:
+                raise AssertionError("characteristic length must be positive")
+            z = np.asarray(zgrid, dtype="d")
+            if z.shape != tuple(P.shape):
+                z = np.broadcast_to(z, tuple(P.shape))
+            z = np.ascontiguousarray(z)
+            flags = _native.REUSE if _same_array(P, ("z", c), z) else 0
+            _native.check(L.hs2g_source_zdecay(P.handle.ptr, c, z.ctypes.data, float(direc[0]), float(offset),
+                                               abs(float(ddz)), float(jpm2), length, float(dt), flags))
+        else:
+            J = src[2]
+            nsel = None
+            if isinstance(J, numbers.Number):
+                Ja = np.array([float(J)])
+            else:
+                Ja = np.ascontiguousarray(np.asarray(J, dtype="d").reshape(-1))
+                if Ja.size != 1:
+                    nsel = int(np.count_nonzero(np.asarray(volumetric_elements) == c))
+                    if Ja.size != nsel:
+                        raise ValueError("point source of class %d has %d values for %d voxels"
+                                         % (c, Ja.size, nsel))
+            flags = _native.REUSE if _same_array(P, ("J", c), Ja) else 0
+            vols, volume = None, 1.0
+            if np.ndim(P.volume_array) > 0:
+                V = np.ascontiguousarray(P.volume_array, dtype="d")
+                if not _same_array(P, ("V", c), V):
+                    flags &= ~_native.REUSE      # joules and volumes are reused together or not at all
+                vols = V.ctypes.data
+            else:
+                volume = float(P.volume_array)
+            _native.check(L.hs2g_source_point(P.handle.ptr, c, Ja.ctypes.data, int(Ja.size), vols, volume,
+                                              float(dt), flags))
+        done[c] = key
 
 
 def source_table(sources, t, dt, volume):
@@ -197,6 +230,14 @@ def _class_map_update(P, volumetric_elements):
 def _class_map_uploaded(P, newmap):
     if newmap is not None:
         P.compiled_volumetric = newmap
+        P.__dict__.pop("_shapes", None)     # the device dropped every source shape with the old map
+
+
+def _upload_class_map(P, newmap):
+    """Replace the device's source-class map before anything that reads it (the source shapes)."""
+    if newmap is not None:
+        _native.check(_native.load().hs2g_set_source_classes(P.handle.ptr, newmap.ctypes.data, 0))
+        _class_map_uploaded(P, newmap)
 
 
 def run_adi_steps(ADI_params, ADI_steps, t, dt, Tarray, volumetric_elements, volumetric):
@@ -205,11 +246,8 @@ def run_adi_steps(ADI_params, ADI_steps, t, dt, Tarray, volumetric_elements, vol
     L = _native.load()
     sources = _ClassSources(volumetric, np.ndim(P.volume_array) > 0)
     qtab, active = source_table(sources, t, dt, P.volume_array)
-    ve = volumetric_elements
-    qdense = _dense_source(P.shape, P.volume_array, t, dt, np.asarray(ve), sources.dense) if sources.dense else None
-    newmap = _class_map_update(P, ve) if active else None
-    qptr = qtab.ctypes.data if active else None
-    if _is_torch_cuda(Tarray):
+    on_dev = _is_torch_cuda(Tarray)
+    if on_dev:
         import torch
         T = Tarray
         if T.dtype != torch.float64:
@@ -219,36 +257,33 @@ def run_adi_steps(ADI_params, ADI_steps, t, dt, Tarray, volumetric_elements, vol
         if T.device.index != P.device:
             raise ValueError("Tarray is on cuda:%d, the problem on cuda:%d" % (T.device.index, P.device))
         T = T.contiguous()
-        out = torch.empty_like(T)
-        qd = None
-        if qdense is not None:
-            qd = torch.from_numpy(qdense).to(T.device)
         stream = torch.cuda.current_stream(T.device)
         _native.check(L.hs2g_set_stream(P.handle.ptr, ctypes.c_void_p(stream.cuda_stream)))
-        _native.check(L.hs2g_step(P.handle.ptr, T.data_ptr(), out.data_ptr(), qptr,
-                                  qd.data_ptr() if qd is not None else None,
-                                  newmap.ctypes.data if newmap is not None else None, _native.DEVICE))
-        _class_map_uploaded(P, newmap)
-        if qd is not None:
-            qd.record_stream(stream)
+    else:
+        T = np.ascontiguousarray(Tarray, dtype="d")
+        if T.shape != tuple(P.shape):
+            raise ValueError("Tarray has shape %s, expected %s" % (T.shape, tuple(P.shape)))
+        _native.check(L.hs2g_set_stream(P.handle.ptr, None))
+    if active:
+        # the step's sources read the device's class map (and, for shaped classes, their shapes): both are
+        # brought up to date first, on the step's stream
+        _upload_class_map(P, _class_map_update(P, volumetric_elements))
+        _prepare_shapes(P, sources, (t,), dt, volumetric_elements)
+    qptr = qtab.ctypes.data if active else None
+    if on_dev:
+        out = torch.empty_like(T)
+        _native.check(L.hs2g_step(P.handle.ptr, T.data_ptr(), out.data_ptr(), qptr, None, None, _native.DEVICE))
         return out
-    T = np.ascontiguousarray(Tarray, dtype="d")
-    if T.shape != tuple(P.shape):
-        raise ValueError("Tarray has shape %s, expected %s" % (T.shape, tuple(P.shape)))
     out = np.empty_like(T)
-    _native.check(L.hs2g_set_stream(P.handle.ptr, None))
-    _native.check(L.hs2g_step(P.handle.ptr, T.ctypes.data, out.ctypes.data, qptr,
-                              qdense.ctypes.data if qdense is not None else None,
-                              newmap.ctypes.data if newmap is not None else None, 0))
-    _class_map_uploaded(P, newmap)
+    _native.check(L.hs2g_step(P.handle.ptr, T.ctypes.data, out.ctypes.data, qptr, None, None, 0))
     return out
 
 
 def run(ADI_params, Tarray, times, dt, volumetric_elements, volumetric, record_layer=None, record_surface=False):
     """Advance ``Tarray`` through one step per value in ``times`` (the t passed to each step), on the device.
 
-    Equivalent to calling run_adi_steps once per t, but steps without per-voxel sources are queued in one
-    native call.  Returns ``T``, or ``(T, history)`` of shape (len(times), ny, nx) recorded after every step:
+    Equivalent to calling run_adi_steps once per t, with every step queued in one native call (the per-voxel
+    source kinds included: their shapes are evaluated on the device before the first step).  Returns ``T``, or ``(T, history)`` of shape (len(times), ny, nx) recorded after every step:
     the layer z=record_layer with ``record_layer``, or with ``record_surface=True`` the z = 0 surface
     temperature as the reference's ``insulating_z_min_surface_temperature(T, dz)`` estimates it
     (heatsim2_gb300.surface_temperature)."""
@@ -279,61 +314,24 @@ def run(ADI_params, Tarray, times, dt, volumetric_elements, volumetric, record_l
         _native.check(L.hs2g_set_stream(P.handle.ptr, None))
         ptr = T.ctypes.data
         flags = 0
-    ve = np.asarray(volumetric_elements)
     qtabs = np.zeros((n, _native.MAX_CLASSES))
-    dense_steps = {}
     any_active = False
     for s, t in enumerate(times):
         qtabs[s], act = source_table(sources, t, dt, P.volume_array)
         any_active |= act
-        if sources.dense:
-            qd = _dense_source(P.shape, P.volume_array, t, dt, ve, sources.dense)
-            if qd is not None:
-                dense_steps[s] = qd
-    # a changed source-class map is uploaded with the first step (run on its own for that reason)
-    newmap = _class_map_update(P, ve) if (any_active or dense_steps) else None
-    s = 0
-    first = True
-    while s < n:
-        if s in dense_steps or (first and newmap is not None):
-            qd = dense_steps.get(s)
-            if on_dev and qd is not None:
-                qd = torch.from_numpy(qd).to(T.device)
-                qdp = qd.data_ptr()
-            else:
-                qdp = qd.ctypes.data if qd is not None else None
-            _native.check(L.hs2g_step(P.handle.ptr, ptr, ptr, qtabs[s].ctypes.data, qdp,
-                                      newmap.ctypes.data if (first and newmap is not None) else None,
-                                      flags | _native.SYNC))
-            if first:
-                _class_map_uploaded(P, newmap)
-            if hist is not None:
-                if record_surface:
-                    from .surface_temperature import insulating_z_min_surface_temperature
-                    hist[s] = insulating_z_min_surface_temperature(T, dz)
-                else:
-                    hist[s] = T[record_layer]
-            s += 1
-            first = False
-            continue
-        e = s
-        while e < n and e not in dense_steps:
-            e += 1
-        chunk = np.ascontiguousarray(qtabs[s:e])
-        if hist is not None:
-            hbuf = hist[s:e] if on_dev else np.empty((e - s, ny, nx))
-            hptr = hbuf.data_ptr() if on_dev else hbuf.ctypes.data
-            if record_surface:
-                _native.check(L.hs2g_run_surface(P.handle.ptr, e - s, ptr, ptr, chunk.ctypes.data, dz, hptr, flags))
-            else:
-                _native.check(L.hs2g_run(P.handle.ptr, e - s, ptr, ptr, chunk.ctypes.data, int(record_layer), hptr,
-                                         flags))
-            if not on_dev:
-                hist[s:e] = hbuf
+    if any_active:
+        # a changed source-class map and the shapes of the shaped classes that fire within the run are set on
+        # the device first; the steps then run in one native call, firing steps included
+        _upload_class_map(P, _class_map_update(P, volumetric_elements))
+        _prepare_shapes(P, sources, times, dt, volumetric_elements)
+    if hist is not None:
+        hptr = hist.data_ptr() if on_dev else hist.ctypes.data
+        if record_surface:
+            _native.check(L.hs2g_run_surface(P.handle.ptr, n, ptr, ptr, qtabs.ctypes.data, dz, hptr, flags))
         else:
-            _native.check(L.hs2g_run(P.handle.ptr, e - s, ptr, ptr, chunk.ctypes.data, 0, None, flags))
-        s = e
-        first = False
+            _native.check(L.hs2g_run(P.handle.ptr, n, ptr, ptr, qtabs.ctypes.data, int(record_layer), hptr, flags))
+    else:
+        _native.check(L.hs2g_run(P.handle.ptr, n, ptr, ptr, qtabs.ctypes.data, 0, None, flags))
     if on_dev:
         stream.synchronize()
     return (T, hist) if recording else T

@@ -107,7 +107,7 @@ class Batch(object):
         """Per-step source tables for the t values ``times`` (one step each) with each instance's own
         ``volumetric`` tuple and class map; resets the step clock."""
         srcs = [_ClassSources(p.volumetric) for p in self.problems]
-        if any(s.dense for s in srcs):
+        if any(s.shaped for s in srcs):
             raise NotImplementedError("per-voxel sources (point joules with an array, z-decaying impulse) are "
                                       "not provided in the batched form")
         nclass = max(1, max(len(p.volumetric) for p in self.problems))

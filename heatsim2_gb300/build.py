@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "libhs2g.so")
 BUILD_DIR = os.path.join(HERE, "_build")
 SOURCES = ["hs2g_api.cu", "hs2g_compile.cu", "hs2g_sweep.cu", "hs2g_lines.cu", "hs2g_static.cu", "hs2g_batch.cu",
-           "hs2g_adjoint.cu"]
+           "hs2g_adjoint.cu", "hs2g_sources.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

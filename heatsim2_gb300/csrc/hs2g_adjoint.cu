@@ -112,6 +112,47 @@ __global__ void adj_setup_kernel(AView v, const double* __restrict__ k, const do
   M[p] = C[p] * inv_dt;
 }
 
+// A fixed-temperature voxel gets this capacity: its row of every stage matrix is then M times the identity to
+// within 1e-290, its increments vanish against T, and the stage matrices stay symmetric (the reference's
+// identity rows with couplings from computed neighbours are not), so the adjoint's transposed solves remain
+// the forward solves.
+constexpr double kFixedCapacity = 1e300;
+
+// The same with face classes and fixed voxels: the conductance of a face of class c on axis a is the class's
+// affine form f0 + flo k_lo + fhi k_hi, the k of a fixed side replaced by its computed neighbour's
+// (crank_nicolson.pyx:298-338); a face between two fixed voxels conducts nothing.  A class index past the
+// table records an error.
+__global__ void adj_setup_faces_kernel(AView v, const double* __restrict__ k, const double* __restrict__ C,
+                                       double inv_dt, const uint8_t* __restrict__ fcls, int nclass,
+                                       const double* __restrict__ forms, const uint8_t* __restrict__ fixed,
+                                       double* __restrict__ gx, double* __restrict__ gy, double* __restrict__ gz,
+                                       double* __restrict__ M, int* __restrict__ err) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= v.nvox) return;
+  const Vox x = vox_at(v, p);
+  const bool fp = fixed && fixed[p];
+  M[p] = fp ? kFixedCapacity : C[p] * inv_dt;
+  double* out[3] = {gz, gy, gx};
+  const bool has_low[3] = {x.k > 0, x.j > 0, x.i > 0};
+  const int64_t step[3] = {x.nxy, x.nx, 1};
+  for (int a = 0; a < 3; ++a) {
+    double G = 0.0;
+    if (has_low[a]) {
+      const int64_t q = p - step[a];
+      const bool fq = fixed && fixed[q];
+      const int c = fcls[a * v.nvox + p];
+      if (c >= nclass) {
+        atomicExch(err, 1);
+      } else if (!(fp && fq)) {
+        const double* f = forms + ((int64_t)(x.inst * nclass + c) * 3 + a) * 3;
+        const double klo = fq ? k[p] : k[q], khi = fp ? k[q] : k[p];
+        G = fma(f[2], khi, fma(f[1], klo, f[0]));
+      }
+    }
+    out[a][p] = G;
+  }
+}
+
 // D = the sum of a voxel's six face conductances (the diagonal of -L)
 __global__ void adj_diag_kernel(AView v, const double* __restrict__ gx, const double* __restrict__ gy,
                                 const double* __restrict__ gz, double* __restrict__ D) {
@@ -736,6 +777,46 @@ __global__ void adj_chain_kernel(AView v, const double* __restrict__ ggx, const 
   gC[p] = gM[p] * inv_dt;
 }
 
+// The chain with face classes: d G_f / d k of each side from the face's affine form (both coefficients to the
+// computed side of a face with a fixed neighbour); no gradient for fixed voxels' k, C and q.
+__global__ void adj_chain_faces_kernel(AView v, const double* __restrict__ ggx, const double* __restrict__ ggy,
+                                       const double* __restrict__ ggz, const double* __restrict__ gM, double inv_dt,
+                                       const uint8_t* __restrict__ fcls, int nclass, const double* __restrict__ forms,
+                                       const uint8_t* __restrict__ fixed, double* __restrict__ gk,
+                                       double* __restrict__ gC, double* __restrict__ gq) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= v.nvox) return;
+  const Vox x = vox_at(v, p);
+  const bool fp = fixed && fixed[p];
+  if (fp) {
+    gk[p] = 0.0;
+    gC[p] = 0.0;
+    gq[p] = 0.0;
+    return;
+  }
+  const double* gg[3] = {ggz, ggy, ggx};
+  const int64_t coord[3] = {x.k, x.j, x.i}, len[3] = {x.nz, x.ny, x.nx}, step[3] = {x.nxy, x.nx, 1};
+  double acc = 0.0;
+  for (int a = 0; a < 3; ++a) {
+    if (coord[a] > 0) {  // low face: p is its hi side
+      const int64_t q = p - step[a];
+      const int c = min((int)fcls[a * v.nvox + p], nclass - 1);
+      const double* f = forms + ((int64_t)(x.inst * nclass + c) * 3 + a) * 3;
+      const bool fq = fixed && fixed[q];
+      acc = fma(gg[a][p], fq ? f[1] + f[2] : f[2], acc);
+    }
+    if (coord[a] + 1 < len[a]) {  // high face (the low face of r): p is its lo side
+      const int64_t r = p + step[a];
+      const int c = min((int)fcls[a * v.nvox + r], nclass - 1);
+      const double* f = forms + ((int64_t)(x.inst * nclass + c) * 3 + a) * 3;
+      const bool fr = fixed && fixed[r];
+      acc = fma(gg[a][r], fr ? f[1] + f[2] : f[1], acc);
+    }
+  }
+  gk[p] = acc;
+  gC[p] = gM[p] * inv_dt;
+}
+
 }  // namespace
 }  // namespace hs2g
 
@@ -758,6 +839,13 @@ struct hs2g_adjoint {
   // parameters and derived fields
   double *k = nullptr, *C = nullptr, *q = nullptr, *M = nullptr, *D = nullptr;
   double* g[3] = {nullptr, nullptr, nullptr};
+  // face classes and fixed voxels (hs2g_adjoint_set_faces): without them every interior face conducts with the
+  // arithmetic mean of k and every voxel is computed
+  uint8_t* fcls = nullptr;   // 3 * n: class of each voxel's low face on z, y, x
+  uint8_t* fixed = nullptr;  // n, or null
+  double* forms = nullptr;   // [ninst][nclass][3][3]
+  int nclass = 0;
+  int* err = nullptr;
   // line factors of A_x, A_y, A_z: e = lo / piv, u = super-diagonal / piv, ip = 1 / piv
   double *e[3] = {nullptr, nullptr, nullptr}, *u[3] = {nullptr, nullptr, nullptr},
          *ip[3] = {nullptr, nullptr, nullptr};
@@ -918,7 +1006,7 @@ void adj_free(hs2g_adjoint* a) {
   void* ptrs[] = {a->inst, a->vox_off, a->line_off, a->xg_off, a->k, a->C, a->q, a->M, a->D, a->g[0], a->g[1],
                   a->g[2], a->e[0], a->e[1], a->e[2], a->u[0], a->u[1], a->u[2], a->ip[0], a->ip[1], a->ip[2],
                   a->obs, a->ckpts, a->seg, a->seg2, a->T, a->lam, a->mu[0], a->mu[1], a->mu[2], a->gg[0], a->gg[1],
-                  a->gg[2], a->gM, a->gq, a->parts};
+                  a->gg[2], a->gM, a->gq, a->parts, a->fcls, a->fixed, a->forms, a->err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (a->ev0) cudaEventDestroy(a->ev0);
@@ -1092,7 +1180,14 @@ int hs2g_adjoint_set_parameters(hs2g_adjoint* a, const double* k, const double* 
   if (e == cudaSuccess) e = cudaMemcpyAsync(a->q, q, sizeof(double) * n, kind, st);
   if (e != cudaSuccess) return acuda(e, "hs2g_adjoint_set_parameters");
   const hs2g::AView v = view(a);
-  hs2g::adj_setup_kernel<<<nblk(n), kTh, 0, st>>>(v, a->k, a->C, 1.0 / a->dt, a->g[0], a->g[1], a->g[2], a->M);
+  if (a->forms) {
+    e = cudaMemsetAsync(a->err, 0, sizeof(int), st);
+    if (e != cudaSuccess) return acuda(e, "hs2g_adjoint_set_parameters");
+    hs2g::adj_setup_faces_kernel<<<nblk(n), kTh, 0, st>>>(v, a->k, a->C, 1.0 / a->dt, a->fcls, a->nclass, a->forms,
+                                                          a->fixed, a->g[0], a->g[1], a->g[2], a->M, a->err);
+  } else {
+    hs2g::adj_setup_kernel<<<nblk(n), kTh, 0, st>>>(v, a->k, a->C, 1.0 / a->dt, a->g[0], a->g[1], a->g[2], a->M);
+  }
   hs2g::adj_diag_kernel<<<nblk(n), kTh, 0, st>>>(v, a->g[0], a->g[1], a->g[2], a->D);
   for (int ax = 0; ax < 3; ++ax)
     hs2g::adj_factor_kernel<<<nblk(a->nlines[ax]), kTh, 0, st>>>(v, ax, a->nlines[ax], a->M, a->g[ax], a->e[ax],
@@ -1100,7 +1195,70 @@ int hs2g_adjoint_set_parameters(hs2g_adjoint* a, const double* k, const double* 
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return acuda(e, "hs2g_adjoint_set_parameters");
+  if (a->forms) {
+    int bad = 0;
+    e = cudaMemcpy(&bad, a->err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return acuda(e, "hs2g_adjoint_set_parameters");
+    if (bad) return afail(HS2G_ERR_ARG, "hs2g_adjoint_set_parameters: a face class index is past the forms table");
+  }
   a->have_params = true;
+  return HS2G_OK;
+}
+
+int hs2g_adjoint_set_faces(hs2g_adjoint* a, int nclass, const double* forms, const uint8_t* face_z,
+                           const uint8_t* face_y, const uint8_t* face_x, const uint8_t* fixed, int flags) {
+  if (a && nclass == 0) {  // back to the default: every interior face conducting, every voxel computed
+    AGuard guard(a->device);
+    cudaStreamSynchronize(a->stream);
+    void* ptrs[] = {a->forms, a->fcls, a->fixed};
+    for (void* p : ptrs)
+      if (p) cudaFree(p);
+    a->forms = nullptr;
+    a->fcls = a->fixed = nullptr;
+    a->nclass = 0;
+    a->have_params = false;
+    a->nsteps = 0;
+    a->stored_seg = -1;
+    return HS2G_OK;
+  }
+  if (!a || nclass < 1 || nclass > HS2G_MAX_CLASSES || !forms || !face_z || !face_y || !face_x)
+    return afail(HS2G_ERR_ARG, "hs2g_adjoint_set_faces: bad argument");
+  const int64_t nf = (int64_t)a->ninst * nclass * 9;
+  for (int64_t t = 0; t < nf; ++t)
+    if (!std::isfinite(forms[t])) return afail(HS2G_ERR_ARG, "hs2g_adjoint_set_faces: non-finite face form");
+  AGuard guard(a->device);
+  cudaStream_t st = a->stream;
+  const int64_t n = a->n;
+  const cudaMemcpyKind kind = in_kind(flags);
+  cudaError_t e = cudaSuccess;
+  if (a->forms && a->nclass != nclass) {
+    cudaFree(a->forms);
+    a->forms = nullptr;
+  }
+  if (!a->forms) e = cudaMalloc(&a->forms, sizeof(double) * nf);
+  if (e == cudaSuccess && !a->fcls) e = cudaMalloc(&a->fcls, 3 * (size_t)n);
+  if (e == cudaSuccess && !a->err) e = cudaMalloc(&a->err, sizeof(int));
+  if (e == cudaSuccess && fixed && !a->fixed) e = cudaMalloc(&a->fixed, (size_t)n);
+  if (e != cudaSuccess) {
+    cudaFree(a->forms);
+    a->forms = nullptr;
+    return acuda(e, "hs2g_adjoint_set_faces: device allocation");
+  }
+  a->nclass = nclass;
+  e = cudaMemcpyAsync(a->forms, forms, sizeof(double) * nf, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(a->fcls, face_z, (size_t)n, kind, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(a->fcls + n, face_y, (size_t)n, kind, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(a->fcls + 2 * n, face_x, (size_t)n, kind, st);
+  if (e == cudaSuccess && fixed) e = cudaMemcpyAsync(a->fixed, fixed, (size_t)n, kind, st);
+  if (e == cudaSuccess && !fixed && a->fixed) {
+    cudaFree(a->fixed);
+    a->fixed = nullptr;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return acuda(e, "hs2g_adjoint_set_faces");
+  a->have_params = false;  // the faces apply from the next hs2g_adjoint_set_parameters
+  a->nsteps = 0;
+  a->stored_seg = -1;
   return HS2G_OK;
 }
 
@@ -1251,8 +1409,13 @@ int hs2g_adjoint_backward(hs2g_adjoint* a, double* gk, double* gC, double* gq, d
     if (e == cudaSuccess && !dbl && sg >= 1) e = recompute(sg - 1);
   }
   if (e == cudaSuccess) {
-    hs2g::adj_chain_kernel<<<nblk(n), kTh, 0, st>>>(v, a->gg[0], a->gg[1], a->gg[2], a->gM, 1.0 / a->dt, a->mu[0],
-                                                    a->mu[1]);
+    if (a->forms)
+      hs2g::adj_chain_faces_kernel<<<nblk(n), kTh, 0, st>>>(v, a->gg[0], a->gg[1], a->gg[2], a->gM, 1.0 / a->dt,
+                                                            a->fcls, a->nclass, a->forms, a->fixed, a->mu[0],
+                                                            a->mu[1], a->gq);
+    else
+      hs2g::adj_chain_kernel<<<nblk(n), kTh, 0, st>>>(v, a->gg[0], a->gg[1], a->gg[2], a->gM, 1.0 / a->dt,
+                                                      a->mu[0], a->mu[1]);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaEventRecord(a->ev1, st);

@@ -51,6 +51,15 @@ struct hs2g_handle {
   double* qdense_dev = nullptr;
   double* hist_dev = nullptr;
   int64_t hist_len = 0;
+  // per-voxel source shapes (hs2g_source_zdecay / hs2g_source_point): the multiplier field, which classes
+  // have one, the device copies of their z coordinates / joules / cell volumes, and the rank-scan scratch
+  double* qshape = nullptr;
+  bool shaped[HS2G_MAX_CLASSES] = {};
+  double* shape_zgrid[HS2G_MAX_CLASSES] = {};
+  double* shape_joules[HS2G_MAX_CLASSES] = {};
+  int64_t shape_joules_len[HS2G_MAX_CLASSES] = {};
+  double* shape_volumes = nullptr;
+  int64_t* shape_tiles = nullptr;
   unsigned long long* err_dev = nullptr;
   int* status_dev = nullptr;
   bool bulk_y = false, bulk_z = false;
@@ -169,8 +178,21 @@ int check_kernel_error(hs2g_handle* h) {
               (long long)i);
 }
 
+// Row pitch of the y sweep's arrays: nx rounded up to an even count, so that TMA tile rows start on 16-byte
+// boundaries whatever nx is (HS2G_ROW_PITCH=<multiple> pads further, for tests of the padded layout).
+int64_t y_pitch(int64_t nx) {
+  int64_t m = 2;
+  if (const char* e = getenv("HS2G_ROW_PITCH")) {
+    const long long v = atoll(e);
+    if (v >= 2 && v % 2 == 0 && v <= 1024) m = v;
+  }
+  return (nx + m - 1) / m * m;
+}
+
 int alloc_common(hs2g_handle* h, bool faces = true) {
   const int64_t n = h->d.nvox();
+  h->c.px = y_pitch(h->d.nx);
+  const int64_t np = h->d.nz * h->d.ny * h->c.px;  // voxels of the padded y-sweep arrays
   int rc;
   if (faces && (rc = dalloc(h, &h->Gz, (h->d.nz + 1) * h->d.nxy(), "Gz"))) return rc;
   if (faces && (rc = dalloc(h, &h->Gy, h->d.nz * (h->d.ny + 1) * h->d.nx, "Gy"))) return rc;
@@ -178,9 +200,9 @@ int alloc_common(hs2g_handle* h, bool faces = true) {
   if ((rc = dalloc(h, &h->M, n, "capacity"))) return rc;
   if ((rc = dalloc(h, &h->compute, n, "compute mask"))) return rc;
   if ((rc = dalloc(h, &h->vclass, n, "source classes"))) return rc;
-  if ((rc = dalloc(h, &h->W0, n, "stage buffer 0"))) return rc;
-  if ((rc = dalloc(h, &h->W1, n, "stage buffer 1"))) return rc;
-  if ((rc = dalloc(h, &h->coef_block, n * hs2g::kNumCoeffArrays, "step coefficients"))) return rc;
+  if ((rc = dalloc(h, &h->W0, np, "stage buffer 0"))) return rc;
+  if ((rc = dalloc(h, &h->W1, np, "stage buffer 1"))) return rc;
+  if ((rc = dalloc(h, &h->coef_block, np * hs2g::kNumCoeffArrays, "step coefficients"))) return rc;
   h->c.nchunks = (h->d.nx + 31) / 32;
   h->xb_len = h->d.nz * h->d.ny * h->c.nchunks * hs2g::kXBlockCoeffs * 32;
   if ((rc = dalloc(h, &h->c.xb, h->xb_len, "x stencil coefficients"))) return rc;
@@ -188,7 +210,7 @@ int alloc_common(hs2g_handle* h, bool faces = true) {
   if ((rc = dalloc(h, &h->err_dev, 1, "error word"))) return rc;
   if ((rc = dalloc(h, &h->status_dev, 1, "status word"))) return rc;
   double** slots[hs2g::kNumCoeffArrays] = {&h->c.a0, &h->c.b0, &h->c.a1, &h->c.b1, &h->c.a2, &h->c.b2};
-  for (int s = 0; s < hs2g::kNumCoeffArrays; ++s) *slots[s] = h->coef_block + (int64_t)s * n;
+  for (int s = 0; s < hs2g::kNumCoeffArrays; ++s) *slots[s] = h->coef_block + (int64_t)s * np;
   HS2G_CUDA(cudaMemsetAsync(h->err_dev, 0, sizeof(unsigned long long), h->stream), "clear error word");
   HS2G_CUDA(cudaMemsetAsync(h->status_dev, 0, sizeof(int), h->stream), "clear status word");
   // tensor-tile line sweeps need 16-byte aligned coefficient arrays (an even voxel count) and even row pitches
@@ -197,8 +219,10 @@ int alloc_common(hs2g_handle* h, bool faces = true) {
   // and testing): HS2G_LINE_SWEEP=plain the plain-load y sweep, HS2G_Z_SWEEP=tma the TMA tensor-tile z sweep.
   const char* ymode = getenv("HS2G_LINE_SWEEP");
   const char* zmode = getenv("HS2G_Z_SWEEP");
-  h->bulk_y = !(ymode && strcmp(ymode, "plain") == 0) && (n % 2 == 0) && hs2g::lines_bulk_supported(h->d, 1);
-  h->bulk_z = (zmode && strcmp(zmode, "tma") == 0) && (n % 2 == 0) && hs2g::lines_bulk_supported(h->d, 2);
+  h->bulk_y = !(ymode && strcmp(ymode, "plain") == 0) && hs2g::lines_bulk_supported(h->d, 1, h->c.px);
+  h->bulk_z = (zmode && strcmp(zmode, "tma") == 0) && h->c.px == h->d.nx && (n % 2 == 0) &&
+              hs2g::lines_bulk_supported(h->d, 2, h->d.nx);
+
   h->tmaps = hs2g::tensor_map_cache_create();
   return HS2G_OK;
 }
@@ -334,6 +358,56 @@ int step_host_pipelined(hs2g_handle* h, hs2g::StepArgs& a, const hs2g::QTable& q
   return check_status(h);
 }
 
+// The shape field applies to a step whose table gives a shaped class a non-zero value.
+const double* active_shape(const hs2g_handle* h, const double* qtab) {
+  if (!h->qshape || !qtab) return nullptr;
+  for (int c = 0; c < HS2G_MAX_CLASSES; ++c)
+    if (h->shaped[c] && qtab[c] != 0.0) return h->qshape;
+  return nullptr;
+}
+
+// A new source-class map invalidates every shape: reset the field to 1 and forget which classes had one.
+int reset_shapes(hs2g_handle* h) {
+  for (int c = 0; c < HS2G_MAX_CLASSES; ++c) h->shaped[c] = false;
+  if (h->qshape) HS2G_CUDA(hs2g::launch_fill(h->qshape, h->d.nvox(), 1.0, h->stream), "reset source shapes");
+  return HS2G_OK;
+}
+
+int ensure_shape(hs2g_handle* h) {
+  if (h->qshape) return HS2G_OK;
+  int rc = dalloc(h, &h->qshape, h->d.nvox(), "source shape");
+  if (rc) return rc;
+  HS2G_CUDA(hs2g::launch_fill(h->qshape, h->d.nvox(), 1.0, h->stream), "initialise source shape");
+  return HS2G_OK;
+}
+
+// The device copy of a per-voxel input of a shaped class: the caller's pointer (HS2G_DEVICE), the copy kept
+// from the previous call (HS2G_REUSE), or a fresh upload into the handle's buffer.
+int shape_input(hs2g_handle* h, double** buf, int64_t* buf_len, int64_t len, const double* src, int flags,
+                const char* what, const double** out) {
+  if (flags & HS2G_DEVICE) {
+    *out = src;
+    return HS2G_OK;
+  }
+  if (flags & HS2G_REUSE) {
+    if (!*buf || *buf_len != len) return fail(HS2G_ERR_STATE, "%s: nothing to reuse (no earlier upload of %lld values)", what, (long long)len);
+    *out = *buf;
+    return HS2G_OK;
+  }
+  if (*buf && *buf_len != len) {
+    dfree(h, *buf, *buf_len);
+    *buf_len = 0;
+  }
+  if (!*buf) {
+    int rc = dalloc(h, buf, len, what);
+    if (rc) return rc;
+    *buf_len = len;
+  }
+  HS2G_CUDA(cudaMemcpyAsync(*buf, src, sizeof(double) * len, cudaMemcpyHostToDevice, h->stream), what);
+  *out = *buf;
+  return HS2G_OK;
+}
+
 }  // namespace
 
 int hs2g::set_last_error(int code, const char* message) { return fail(code, "%s", message); }
@@ -359,14 +433,22 @@ void hs2g_destroy(hs2g_handle* h) {
   dfree(h, h->M, n);
   dfree(h, h->compute, n);
   dfree(h, h->vclass, n);
-  dfree(h, h->coef_block, 0);
+  const int64_t np = h->d.nz * h->d.ny * h->c.px;
+  dfree(h, h->coef_block, np * hs2g::kNumCoeffArrays);
   dfree(h, h->c.xb, h->xb_len);
-  dfree(h, h->W0, n);
-  dfree(h, h->W1, n);
+  dfree(h, h->W0, np);
+  dfree(h, h->W1, np);
   dfree(h, h->Tin_dev, n);
   dfree(h, h->Tout_dev, n);
   dfree(h, h->qdense_dev, n);
   dfree(h, h->hist_dev, 0);
+  dfree(h, h->qshape, n);
+  for (int c = 0; c < HS2G_MAX_CLASSES; ++c) {
+    dfree(h, h->shape_zgrid[c], n);
+    dfree(h, h->shape_joules[c], h->shape_joules_len[c]);
+  }
+  dfree(h, h->shape_volumes, n);
+  dfree(h, h->shape_tiles, hs2g::point_shape_tiles(n));
   dfree(h, h->err_dev, 1);
   if (h->copy_stream) {
     cudaStreamSynchronize(h->copy_stream);
@@ -625,6 +707,9 @@ int hs2g_source_table(int nsrc, const int32_t* kind, const double* params, doubl
       case HS2G_IMPULSE_POINT_SOURCE_JOULES:  // joules per element / (volume * dt) (pyx:307-319)
         if (t == a[0]) q = a[1] / (volume * dt);
         break;
+      case HS2G_SHAPED_IMPULSE:  // per-voxel value from the handle's source shape, at t == t0 exactly
+        if (t == a[0]) q = 1.0;
+        break;
       default:
         return fail(HS2G_ERR_ARG, "source class %d has kind %d, which is not evaluated per class", c, kind[c]);
     }
@@ -643,7 +728,11 @@ int hs2g_step(hs2g_handle* h, const double* T_in, double* T_out, const double* q
   const int64_t n = d.nvox();
   const bool dev = (flags & HS2G_DEVICE) != 0;
   cudaStream_t s = h->stream;
-  if (volumetric) HS2G_CUDA(cudaMemcpyAsync(h->vclass, volumetric, (size_t)n, cudaMemcpyHostToDevice, s), "upload classes");
+  if (volumetric) {
+    HS2G_CUDA(cudaMemcpyAsync(h->vclass, volumetric, (size_t)n, cudaMemcpyHostToDevice, s), "upload classes");
+    int rc = reset_shapes(h);
+    if (rc) return rc;
+  }
   const double* Tin_d = T_in;
   double* Tout_d = T_out;
   if (!dev) {
@@ -663,6 +752,7 @@ int hs2g_step(hs2g_handle* h, const double* T_in, double* T_out, const double* q
   } else {
     memset(&q, 0, sizeof(q));
   }
+  a.qshape = active_shape(h, qtab);
   if (qdense) {
     if (dev) {
       a.qdense = qdense;
@@ -736,12 +826,14 @@ int run_steps(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, con
   memset(&q, 0, sizeof(q));
   for (int st = 0; st < nsteps; ++st) {
     a.has_qtab = false;
+    a.qshape = nullptr;
     if (qtabs) {
       const double* qt = qtabs + (int64_t)st * HS2G_MAX_CLASSES;
       for (int c = 0; c < HS2G_MAX_CLASSES; ++c) {
         q.q[c] = qt[c];
         if (qt[c] != 0.0) a.has_qtab = true;
       }
+      a.qshape = active_shape(h, qt);
     }
     a.T_in = src;
     a.T_out = dst;
@@ -836,12 +928,14 @@ int hs2g_run_timed(hs2g_handle* h, int nsteps, const double* T_in, double* T_out
   int rc = HS2G_OK;
   for (int st = 0; st < nsteps && rc == HS2G_OK; ++st) {
     a.has_qtab = false;
+    a.qshape = nullptr;
     if (qtabs) {
       const double* qt = qtabs + (int64_t)st * HS2G_MAX_CLASSES;
       for (int c = 0; c < HS2G_MAX_CLASSES; ++c) {
         q.q[c] = qt[c];
         if (qt[c] != 0.0) a.has_qtab = true;
       }
+      a.qshape = active_shape(h, qt);
     }
     a.T_in = src;
     a.T_out = T_out;
@@ -900,6 +994,71 @@ int hs2g_get_faces(hs2g_handle* h, double* Gz, double* Gy, double* Gx, double* c
   HS2G_CUDA(cudaStreamSynchronize(s), "get faces");
   if (fixed)
     for (int64_t v = 0; v < n; ++v) fixed[v] = comp[(size_t)v] ? 0 : 1;
+  return HS2G_OK;
+}
+
+int hs2g_set_source_classes(hs2g_handle* h, const uint8_t* volumetric, int flags) {
+  if (!h || !volumetric) return fail(HS2G_ERR_ARG, "null argument");
+  DeviceGuard g(h->device);
+  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", h->device);
+  const cudaMemcpyKind kind = (flags & HS2G_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  HS2G_CUDA(cudaMemcpyAsync(h->vclass, volumetric, (size_t)h->d.nvox(), kind, h->stream), "upload classes");
+  int rc = reset_shapes(h);
+  if (rc) return rc;
+  if (flags & HS2G_SYNC) HS2G_CUDA(cudaStreamSynchronize(h->stream), "upload classes");
+  return HS2G_OK;
+}
+
+int hs2g_source_zdecay(hs2g_handle* h, int cls, const double* zgrid, double direction, double offset, double ddz,
+                       double joules_per_m2, double length, double dt, int flags) {
+  if (!h || (!zgrid && !(flags & HS2G_REUSE))) return fail(HS2G_ERR_ARG, "null argument");
+  if (cls < 0 || cls >= HS2G_MAX_CLASSES) return fail(HS2G_ERR_ARG, "source class %d outside 0..255", cls);
+  if (!(direction == 1.0 || direction == -1.0))
+    return fail(HS2G_ERR_ARG, "the decay direction must be +z or -z (direction +1 or -1)");
+  if (!(length > 0.0) || !(ddz > 0.0) || !(dt > 0.0) || !std::isfinite(offset) || !std::isfinite(joules_per_m2))
+    return fail(HS2G_ERR_ARG, "z-decaying impulse: length, ddz and dt must be positive, offset and J finite");
+  DeviceGuard g(h->device);
+  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", h->device);
+  const int64_t n = h->d.nvox();
+  int rc = ensure_shape(h);
+  if (rc) return rc;
+  int64_t len = h->shape_zgrid[cls] ? n : 0;
+  const double* z = nullptr;
+  if ((rc = shape_input(h, &h->shape_zgrid[cls], &len, n, zgrid, flags, "z coordinates", &z))) return rc;
+  HS2G_CUDA(hs2g::launch_zdecay_shape(n, h->vclass, cls, z, direction, offset, ddz, joules_per_m2, length, dt,
+                                      h->qshape, h->stream),
+            "z-decaying source shape");
+  h->shaped[cls] = true;
+  if (flags & HS2G_SYNC) HS2G_CUDA(cudaStreamSynchronize(h->stream), "z-decaying source shape");
+  return HS2G_OK;
+}
+
+int hs2g_source_point(hs2g_handle* h, int cls, const double* joules, int64_t count, const double* volumes,
+                      double volume, double dt, int flags) {
+  if (!h || (!joules && !(flags & HS2G_REUSE)) || count < 1) return fail(HS2G_ERR_ARG, "bad argument");
+  if (cls < 0 || cls >= HS2G_MAX_CLASSES) return fail(HS2G_ERR_ARG, "source class %d outside 0..255", cls);
+  if (!(dt > 0.0) || (!volumes && !(volume > 0.0)))
+    return fail(HS2G_ERR_ARG, "point source: dt and the cell volume must be positive");
+  DeviceGuard g(h->device);
+  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", h->device);
+  const int64_t n = h->d.nvox();
+  int rc = ensure_shape(h);
+  if (rc) return rc;
+  if (!h->shape_tiles && (rc = dalloc(h, &h->shape_tiles, hs2g::point_shape_tiles(n), "rank scan"))) return rc;
+  const double* J = nullptr;
+  if ((rc = shape_input(h, &h->shape_joules[cls], &h->shape_joules_len[cls], count, joules, flags, "joules", &J)))
+    return rc;
+  const double* V = nullptr;
+  if (volumes) {
+    // the per-cell volumes follow the same DEVICE / REUSE rule as the joules
+    int64_t vlen = h->shape_volumes ? n : 0;
+    if ((rc = shape_input(h, &h->shape_volumes, &vlen, n, volumes, flags, "cell volumes", &V))) return rc;
+  }
+  HS2G_CUDA(hs2g::launch_point_shape(n, h->vclass, cls, h->shape_tiles, J, count, V, volume, dt, h->qshape,
+                                     h->stream),
+            "point source shape");
+  h->shaped[cls] = true;
+  if (flags & HS2G_SYNC) HS2G_CUDA(cudaStreamSynchronize(h->stream), "point source shape");
   return HS2G_OK;
 }
 

@@ -621,6 +621,7 @@ int compile_instance(Batch& b, int ib, const hs2g_class_problem& p, double* ws, 
   }
   hs2g::Coeffs c{};
   c.nchunks = I.nchunks;
+  c.px = d.nx;  // the batched sweeps use plain loads on unpadded rows
   const bool f64 = b.precision == 64;
   double* cbase = f64 ? (double*)b.coef : c6;
   const int64_t cstride = f64 ? b.nvox : n;

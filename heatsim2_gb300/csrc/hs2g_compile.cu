@@ -212,21 +212,22 @@ __global__ void factor_z_kernel(Dims d, F g, const double* __restrict__ M, const
 template <class F>
 __global__ void factor_y_kernel(Dims d, F g, const double* __restrict__ M, const uint8_t* __restrict__ compute,
                                 const double* __restrict__ s2, double* __restrict__ sigma, double* __restrict__ a1,
-                                double* __restrict__ b1) {
+                                double* __restrict__ b1, int64_t px) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= d.nz * d.nx) return;
   const int64_t k = t / d.nx, i = t - k * d.nx;
   double u_prev = 0.0, s2_prev = 1.0;
   for (int64_t j = 0; j < d.ny; ++j) {
     const int64_t p = (k * d.ny + j) * d.nx + i;
+    const int64_t pp = (k * d.ny + j) * px + i;  // a1 / b1 row pitch
     const bool comp = compute[p] != 0;
     const RowIn r = stage_row(comp, M[p], comp ? g.ylo(d, p, k, j, i) : 0.0, comp ? g.yhi(d, p, k, j, i) : 0.0);
     const double piv = r.d - u_prev * r.lo;
     const double u = r.hi / piv;
     const double s2p = s2[p];
     sigma[p] = s2p * M[p] / piv;
-    a1[p] = (j > 0) ? s2p * r.lo / (piv * s2_prev) : 0.0;
-    b1[p] = (j + 1 < d.ny) ? s2p * u / s2[p + d.nx] : 0.0;
+    a1[pp] = (j > 0) ? s2p * r.lo / (piv * s2_prev) : 0.0;
+    b1[pp] = (j + 1 < d.ny) ? s2p * u / s2[p + d.nx] : 0.0;
     u_prev = u;
     s2_prev = s2p;
   }
@@ -327,7 +328,8 @@ cudaError_t launch_factor_with(const Dims& d, F g, const double* M, const uint8_
                                double* sigma, const Coeffs& c, cudaStream_t s) {
   const int th = 128;
   factor_z_kernel<F><<<grid_for(d.nxy(), th), th, 0, s>>>(d, g, M, compute, s2, c.a2, c.b2);
-  factor_y_kernel<F><<<grid_for(d.nz * d.nx, th), th, 0, s>>>(d, g, M, compute, s2, sigma, c.a1, c.b1);
+  factor_y_kernel<F><<<grid_for(d.nz * d.nx, th), th, 0, s>>>(d, g, M, compute, s2, sigma, c.a1, c.b1,
+                                                                c.px ? c.px : d.nx);
   factor_x_kernel<F><<<grid_for(d.nz * d.ny, th), th, 0, s>>>(d, g, M, compute, sigma, c);
   return cudaGetLastError();
 }

@@ -22,12 +22,15 @@ struct Dims {
 // The eight stage-0 stencil coefficients are chunk-blocked: for x-line L = k*ny + j and 32-column chunk ch,
 // block (L*nchunks + ch) holds [wc, wxl, wxh, wyl, wyh, wzl, wzh, wq] x 32 columns (2 KB, zero-padded past
 // nx), so a warp's stencil reads one contiguous stream instead of eight.  The other coefficients are
-// (nz, ny, nx) arrays in voxel order.
+// (nz, ny, nx) arrays in voxel order, a1 and b1 (and the stage buffers W0, W1) with row pitch px.
 constexpr int kXBlockCoeffs = 8;
 enum XCoeff { kWc = 0, kWxl, kWxh, kWyl, kWyh, kWzl, kWzh, kWq };
 struct Coeffs {
   double* xb;   // stage-0 stencil blocks, nz*ny*nchunks*8*32 doubles
   int64_t nchunks;
+  // Row pitch of the arrays the y sweep moves with TMA tiles (W0, W1, a1, b1): nx, or nx rounded up so that
+  // the rows start on 16-byte boundaries (an odd nx gets one pad column).  All other arrays have pitch nx.
+  int64_t px;
   double* a0;
   double* b0;
   double* a1;
@@ -68,6 +71,16 @@ cudaError_t launch_validate_rows(const Dims& d, const double* const rows[6], dou
 cudaError_t launch_factor_rows(const Dims& d, const double* const rows[6], const double* M, const uint8_t* compute,
                                double* s2, double* sigma, const Coeffs& c, cudaStream_t s);
 
+// per-voxel source shapes (hs2g_sources.cu)
+cudaError_t launch_fill(double* p, int64_t n, double v, cudaStream_t s);
+cudaError_t launch_zdecay_shape(int64_t n, const uint8_t* vclass, int cls, const double* zgrid, double direction,
+                                double offset, double ddz, double jpm2, double length, double dt, double* shape,
+                                cudaStream_t s);
+int64_t point_shape_tiles(int64_t n);
+cudaError_t launch_point_shape(int64_t n, const uint8_t* vclass, int cls, int64_t* tile_scratch, const double* joules,
+                               int64_t count, const double* volumes, double volume, double dt, double* shape,
+                               cudaStream_t s);
+
 // step kernels (hs2g_sweep.cu)
 struct StepArgs {
   Dims d;
@@ -77,6 +90,7 @@ struct StepArgs {
   double* W1;
   const uint8_t* vclass;
   const double* qdense;  // may be null
+  const double* qshape;  // per-voxel multiplier of the class sources (null: 1 everywhere)
   bool has_qtab;
   int* status;           // device word: 0, or HS2G_ERR_TIMEOUT when a bounded wait in a kernel ran out
   bool bulk_y, bulk_z;   // use the TMA tensor-tile line sweeps (hs2g_lines.cu) for y / z
@@ -87,11 +101,12 @@ struct StepArgs {
 struct TensorMapCache;
 TensorMapCache* tensor_map_cache_create();
 void tensor_map_cache_destroy(TensorMapCache* c);
-bool lines_bulk_supported(const Dims& d, int axis);
+bool lines_bulk_supported(const Dims& d, int axis, int64_t px);
 cudaError_t lines_bulk_prepare();
+// axis 1 (y): A, alpha, scratch, beta and out have row pitch px; axis 2 (z): every array has pitch nx (px = nx)
 cudaError_t launch_lines_bulk(const Dims& d, int axis, const double* A, const double* alpha, double* scratch,
                               const double* beta, const double* T_in, double* out, int* status,
-                              TensorMapCache* cache, cudaStream_t s);
+                              TensorMapCache* cache, cudaStream_t s, int64_t px);
 cudaError_t launch_step(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s);
 // the same three kernels with an event recorded before each and after the last (ev[0..3])
 cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s,

@@ -15,10 +15,12 @@
 // kernel reports HS2G_ERR_TIMEOUT through the status word.
 //
 // Requirements (checked on the host, which otherwise uses the plain kernels of hs2g_sweep.cu): arrays
-// 16-byte aligned and row pitches (nx for y, ny*nx for z) even, so every global stride is a multiple of 16 B.
+// 16-byte aligned and row pitches even, so every global stride is a multiple of 16 B.  The y sweep's arrays are
+// allocated with an even row pitch px (one pad column for an odd nx); the z sweep needs ny*nx even.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -85,12 +87,40 @@ __global__ void wait_selftest_kernel(uint64_t limit_ns, int arrive, int* status)
 }
 
 // 3-D tile load (x = line index within the row, y = row, z = plane); coordinates may lie outside the array.
-__device__ __forceinline__ void tile_load(void* dst, const CUtensorMap* map, int c0, int c1, int c2, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-      "[%5];" ::"r"(saddr(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(saddr(bar))
-      : "memory");
+// HINT: the copy carries an L2 cache policy (evict-first for data read for the last time in the step).
+template <bool HINT = false>
+__device__ __forceinline__ void tile_load(void* dst, const CUtensorMap* map, int c0, int c1, int c2, uint64_t* bar,
+                                          uint64_t policy = 0) {
+  if (HINT)
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint [%0], "
+        "[%1, {%2, %3, %4}], [%5], %6;" ::"r"(saddr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(saddr(bar)), "l"(policy)
+        : "memory");
+  else
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(saddr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(saddr(bar))
+        : "memory");
+}
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+// store of a value the same kernel reads back soon (the forward sweep's scratch): kept in L2 with HINT
+template <bool HINT>
+__device__ __forceinline__ void st_keep(double* p, double v, uint64_t policy) {
+  if (HINT)
+    asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(v), "l"(policy) : "memory");
+  else
+    *p = v;
 }
 
 struct Geometry {
@@ -106,14 +136,14 @@ __host__ __device__ constexpr int num_arrays() {
   return ADD_T ? 3 : 2;
 }
 
-template <bool ADD_T>
+template <bool ADD_T, int SLOTS = kSlots>
 __host__ __device__ constexpr size_t smem_bytes() {
-  return 128 /*alignment slack*/ + (size_t)kSlots * num_arrays<ADD_T>() * kTileBytes + 8 * kSlots + 16;
+  return 128 /*alignment slack*/ + (size_t)SLOTS * num_arrays<ADD_T>() * kTileBytes + 8 * SLOTS + 16;
 }
 
 // Forward inputs A, alpha -> scratch; back inputs scratch, beta (and T_in when ADD_T) -> out.
 // out may equal scratch (y sweep writes W1 in place) and T_in may equal out (in-place timestep).
-template <bool ADD_T>
+template <bool ADD_T, bool HINT = false, int kSlots = hs2g::kSlots>
 __global__ void __launch_bounds__(kNL) line_sweep_tma_kernel(Geometry g, const __grid_constant__ CUtensorMap mA,
                                                              const __grid_constant__ CUtensorMap mAlpha,
                                                              const __grid_constant__ CUtensorMap mScratch,
@@ -145,22 +175,24 @@ __global__ void __launch_bounds__(kNL) line_sweep_tma_kernel(Geometry g, const _
 
   SlotRing ring;  // slot phases; pending slots are tracked by the producer (tid 0), which issues every copy
   const int cx = (int)i0, cz = (int)plane;
+  const uint64_t pol_first = HINT ? policy_evict_first() : 0;
+  const uint64_t pol_last = HINT ? policy_evict_last() : 0;
 
   auto issue_fwd = [&](int64_t q) {  // tile q covers rows [q*kRows, q*kRows + kRows)
     const int s = (int)(q % kSlots);
     const int r0 = (int)(q * kRows);
     mbar_expect_tx(&bars[s], 2u * kTileBytes);
-    tile_load(tile(s, 0), &mA, cx, r0, cz, &bars[s]);
-    tile_load(tile(s, 1), &mAlpha, cx, r0, cz, &bars[s]);
+    tile_load<HINT>(tile(s, 0), &mA, cx, r0, cz, &bars[s], pol_first);
+    tile_load<HINT>(tile(s, 1), &mAlpha, cx, r0, cz, &bars[s], pol_first);
     ring.issued(s);
   };
   auto issue_back = [&](int64_t q) {  // back tile q covers rows [n - (q+1)*kRows, n - q*kRows)
     const int s = (int)(q % kSlots);
     const int r0 = (int)(n - (q + 1) * kRows);
     mbar_expect_tx(&bars[s], (uint32_t)NA * kTileBytes);
-    tile_load(tile(s, 0), &mScratch, cx, r0, cz, &bars[s]);
-    tile_load(tile(s, 1), &mBeta, cx, r0, cz, &bars[s]);
-    if (ADD_T) tile_load(tile(s, 2), &mT, cx, r0, cz, &bars[s]);
+    tile_load<HINT>(tile(s, 0), &mScratch, cx, r0, cz, &bars[s], pol_first);
+    tile_load<HINT>(tile(s, 1), &mBeta, cx, r0, cz, &bars[s], pol_first);
+    if (ADD_T) tile_load<HINT>(tile(s, 2), &mT, cx, r0, cz, &bars[s], pol_first);
     ring.issued(s);
   };
 
@@ -184,7 +216,7 @@ __global__ void __launch_bounds__(kNL) line_sweep_tma_kernel(Geometry g, const _
       for (int rr = 0; rr < kRows; ++rr) {
         if (rr < nr) {
           z = fma(-tAl[rr * kNL + tid], z, tA[rr * kNL + tid]);
-          dst[rr * g.stride] = z;
+          st_keep<HINT>(dst + rr * g.stride, z, pol_last);
         }
       }
     }
@@ -246,8 +278,9 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// (nz, ny, nx) array seen as rows of lines: y sweep {x: nx, y: ny, z: nz}, z sweep {x: ny*nx, y: nz, z: 1}
-bool encode(CUtensorMap* m, const Dims& d, int axis, const void* ptr) {
+// (nz, ny, nx) array seen as rows of lines: y sweep {x: nx, y: ny, z: nz} with row pitch px (px >= nx, the
+// columns past nx never read), z sweep {x: ny*nx, y: nz, z: 1}
+bool encode(CUtensorMap* m, const Dims& d, int axis, const void* ptr, int64_t px) {
   PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[3], strides[2];
@@ -255,8 +288,8 @@ bool encode(CUtensorMap* m, const Dims& d, int axis, const void* ptr) {
     dims[0] = (cuuint64_t)d.nx;
     dims[1] = (cuuint64_t)d.ny;
     dims[2] = (cuuint64_t)d.nz;
-    strides[0] = (cuuint64_t)d.nx * 8;
-    strides[1] = (cuuint64_t)d.nxy() * 8;
+    strides[0] = (cuuint64_t)px * 8;
+    strides[1] = (cuuint64_t)(d.ny * px) * 8;
   } else {
     dims[0] = (cuuint64_t)d.nxy();
     dims[1] = (cuuint64_t)d.nz;
@@ -279,12 +312,12 @@ inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 
 // Per-handle cache of encoded tensor maps, keyed by (array pointer, axis).
 struct TensorMapCache {
   std::map<std::pair<const void*, int>, CUtensorMap> maps;
-  bool get(const Dims& d, int axis, const void* ptr, CUtensorMap* out) {
-    auto key = std::make_pair(ptr, axis);
+  bool get(const Dims& d, int axis, const void* ptr, int64_t px, CUtensorMap* out) {
+    auto key = std::make_pair(ptr, axis);  // one pitch per handle, so the pointer and axis identify the map
     auto it = maps.find(key);
     if (it == maps.end()) {
       CUtensorMap m;
-      if (!encode(&m, d, axis, ptr)) return false;
+      if (!encode(&m, d, axis, ptr, px)) return false;
       if (maps.size() > 64) maps.clear();
       it = maps.emplace(key, m).first;
     }
@@ -296,17 +329,20 @@ struct TensorMapCache {
 TensorMapCache* tensor_map_cache_create() { return new TensorMapCache(); }
 void tensor_map_cache_destroy(TensorMapCache* c) { delete c; }
 
-bool lines_bulk_supported(const Dims& d, int axis) {
+bool lines_bulk_supported(const Dims& d, int axis, int64_t px) {
   if (!encode_fn()) return false;
-  if (axis == 1) return (d.nx % 2 == 0) && d.nx < (1ll << 31) && d.ny < (1ll << 31) && d.nz < (1ll << 31);
+  if (axis == 1) return (px % 2 == 0) && px < (1ll << 31) && d.ny < (1ll << 31) && d.nz < (1ll << 31);
   return (d.nxy() % 2 == 0) && d.nxy() < (1ll << 31) && d.nz < (1ll << 31);
 }
 
 // Raise the dynamic shared-memory limit of the tile kernels on the current device (once per device, before
 // the first launch; called when a handle is created).
 cudaError_t lines_bulk_prepare() {
-  cudaError_t e = cudaFuncSetAttribute(line_sweep_tma_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem_bytes<false>());
+  cudaError_t e = cudaFuncSetAttribute(line_sweep_tma_kernel<false, true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<false>());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(line_sweep_tma_kernel<false, true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem_bytes<false, 3>());
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(line_sweep_tma_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem_bytes<true>());
@@ -315,24 +351,30 @@ cudaError_t lines_bulk_prepare() {
 
 cudaError_t launch_lines_bulk(const Dims& d, int axis, const double* A, const double* alpha, double* scratch,
                               const double* beta, const double* T_in, double* out, int* status,
-                              TensorMapCache* cache, cudaStream_t s) {
+                              TensorMapCache* cache, cudaStream_t s, int64_t px) {
   if (!aligned16(A) || !aligned16(alpha) || !aligned16(scratch) || !aligned16(beta) || !aligned16(out) ||
       (T_in && !aligned16(T_in)) || !cache)
     return cudaErrorMisalignedAddress;
   CUtensorMap mA, mAl, mS, mB, mT;
-  const bool ok = cache->get(d, axis, A, &mA) && cache->get(d, axis, alpha, &mAl) &&
-                  cache->get(d, axis, scratch, &mS) && cache->get(d, axis, beta, &mB) &&
-                  (T_in ? cache->get(d, axis, T_in, &mT) : cache->get(d, axis, A, &mT));
+  if (axis != 1) px = d.nx;
+  const bool ok = cache->get(d, axis, A, px, &mA) && cache->get(d, axis, alpha, px, &mAl) &&
+                  cache->get(d, axis, scratch, px, &mS) && cache->get(d, axis, beta, px, &mB) &&
+                  (T_in ? cache->get(d, axis, T_in, px, &mT) : cache->get(d, axis, A, px, &mT));
   if (!ok) return cudaErrorInvalidValue;
   Geometry g;
   if (axis == 1) {
     g.groups = (d.nx + kNL - 1) / kNL;
-    g.plane_stride = d.nxy();
+    g.plane_stride = d.ny * px;
     g.width = d.nx;
-    g.stride = d.nx;
+    g.stride = px;
     g.nrows = d.ny;
-    line_sweep_tma_kernel<false><<<(unsigned)(d.nz * g.groups), kNL, smem_bytes<false>(), s>>>(
-        g, mA, mAl, mS, mB, mT, scratch, out, status);
+    const char* slots = getenv("HS2G_Y_SLOTS");
+    if (slots && strcmp(slots, "3") == 0)
+      line_sweep_tma_kernel<false, true, 3><<<(unsigned)(d.nz * g.groups), kNL, smem_bytes<false, 3>(), s>>>(
+          g, mA, mAl, mS, mB, mT, scratch, out, status);
+    else
+      line_sweep_tma_kernel<false, true><<<(unsigned)(d.nz * g.groups), kNL, smem_bytes<false>(), s>>>(
+          g, mA, mAl, mS, mB, mT, scratch, out, status);
   } else {
     g.groups = (d.nxy() + kNL - 1) / kNL;
     g.plane_stride = 0;

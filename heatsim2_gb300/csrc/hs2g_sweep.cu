@@ -41,10 +41,23 @@ constexpr int kLineThreads = 128;
 // wc*T + wxl*T[i-1] + wxh*T[i+1] + wyl*T[j-1] + wyh*T[j+1] + wzl*T[k-1] + wzh*T[k+1] (+ wq*Q).
 // Out-of-grid neighbours carry a zero coefficient (exterior faces are insulating): T[p] is read instead.
 // Column i = ch*32 + lane of the chunk; the coefficients come from the line's chunk block.
+// A sweep's forward values are written and read back by the same thread block within microseconds; with
+// every line in flight they add up to more than L2 (136 MB at 65x512x512), so they are stored with an
+// evict-last L2 policy where that keeps them on chip.
+__device__ __forceinline__ uint64_t l2_policy_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ void st_keep(double* p, double v, uint64_t policy) {
+  asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(v), "l"(policy) : "memory");
+}
+
 template <bool HAS_Q>
 __device__ __forceinline__ double stencil_x(const Dims& d, const double* __restrict__ T, const Coeffs& c,
                                             const uint8_t* __restrict__ vclass, const double* __restrict__ qdense,
-                                            const double* sq, int64_t L, int ch, int lane) {
+                                            const double* __restrict__ qshape, const double* sq, int64_t L, int ch,
+                                            int lane) {
   const int64_t i = (int64_t)ch * 32 + lane;
   const int64_t k = L / d.ny, j = L - k * d.ny;
   const int64_t p = L * d.nx + i;
@@ -66,6 +79,7 @@ __device__ __forceinline__ double stencil_x(const Dims& d, const double* __restr
   r = fma(w[kWzh * 32], tzh, r);
   if (HAS_Q) {
     double q = sq[vclass[p]];
+    if (qshape) q *= qshape[p];
     if (qdense) q += qdense[p];
     r = fma(w[kWq * 32], q, r);
   }
@@ -77,12 +91,17 @@ __device__ __forceinline__ double stencil_x(const Dims& d, const double* __restr
 // its own register allocation.  LINES x-lines per CTA: 32 for the whole grid; the host-buffer step's later,
 // smaller slabs take 16 or 8, whose CTAs finish sooner (a CTA's chunk loop, not the GPU's throughput, sets
 // how long a small launch takes).
-template <bool HAS_Q, bool RANGED, int LINES = kXLines>
-__global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d, const double* __restrict__ T, Coeffs c,
-                                                             const uint8_t* __restrict__ vclass,
-                                                             const double* __restrict__ qdense, QTable qt,
-                                                             double* __restrict__ W0, int64_t line_begin,
-                                                             int64_t line_end) {
+// PITCHED: W0 rows have the pitch c.px (padded: odd nx, or padding for tests); otherwise W0 shares T's pitch nx.
+template <bool PITCHED>
+__device__ __forceinline__ int64_t w0_index(const Dims& d, const Coeffs& c, int64_t L, int64_t i) {
+  return PITCHED ? L * c.px + i : L * d.nx + i;
+}
+
+template <bool HAS_Q, bool RANGED, int LINES, bool PITCHED>
+__device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __restrict__ T, const Coeffs& c,
+                                             const uint8_t* __restrict__ vclass, const double* __restrict__ qdense,
+                                             const double* __restrict__ qshape, const QTable& qt,
+                                             double* __restrict__ W0, int64_t line_begin, int64_t line_end) {
   constexpr int kPerWarp = LINES / kXWarps;
   __shared__ double sr[LINES][kXChunk + 1];
   __shared__ double sa[LINES][kXChunk + 1];
@@ -106,7 +125,7 @@ __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d,
       const int64_t L = L0 + l;
       double r = 0.0, a = 0.0;
       if (L < nlines && i < d.nx) {
-        r = stencil_x<HAS_Q>(d, T, c, vclass, qdense, sq, L, ch, lane);
+        r = stencil_x<HAS_Q>(d, T, c, vclass, qdense, qshape, sq, L, ch, lane);
         a = c.a0[L * d.nx + i];
       }
       sr[l][lane] = r;
@@ -128,7 +147,7 @@ __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d,
     for (int ll = 0; ll < kPerWarp; ++ll) {
       const int l = warp * kPerWarp + ll;
       const int64_t L = L0 + l;
-      if (L < nlines && i < d.nx) W0[L * d.nx + i] = sr[l][lane];
+      if (L < nlines && i < d.nx) W0[w0_index<PITCHED>(d, c, L, i)] = sr[l][lane];
     }
     __syncthreads();
   }
@@ -144,7 +163,7 @@ __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d,
       double z = 0.0, b = 0.0;
       if (L < nlines && i < d.nx) {
         const int64_t p = L * d.nx + i;
-        z = W0[p];
+        z = W0[w0_index<PITCHED>(d, c, L, i)];
         b = c.b0[p];
       }
       sr[l][lane] = z;
@@ -166,31 +185,54 @@ __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d,
     for (int ll = 0; ll < kPerWarp; ++ll) {
       const int l = warp * kPerWarp + ll;
       const int64_t L = L0 + l;
-      if (L < nlines && i < d.nx) W0[L * d.nx + i] = sr[l][lane];
+      if (L < nlines && i < d.nx) W0[w0_index<PITCHED>(d, c, L, i)] = sr[l][lane];
     }
     __syncthreads();
   }
+}
+
+// The whole-grid and ranged x sweeps with W0 rows unpadded (even nx): 72 registers with a bound of 6 blocks.
+template <bool HAS_Q, bool RANGED, int LINES = kXLines>
+__global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d, const double* __restrict__ T, Coeffs c,
+                                                             const uint8_t* __restrict__ vclass,
+                                                             const double* __restrict__ qdense,
+                                                             const double* __restrict__ qshape, QTable qt,
+                                                             double* __restrict__ W0, int64_t line_begin,
+                                                             int64_t line_end) {
+  sweep_x_body<HAS_Q, RANGED, LINES, false>(d, T, c, vclass, qdense, qshape, qt, W0, line_begin, line_end);
+}
+// The same with padded W0 rows (odd nx): the separate row index costs registers (80 under the bound of 6
+// blocks, which puts the grid into two waves), so the budget is set directly to the 72 that keep 7 CTAs per SM
+// (365 us at 65x512x511 against 338 us for the unpadded kernel at 65x512x512).
+template <bool HAS_Q, bool RANGED, int LINES = kXLines>
+__global__ void __maxnreg__(72) sweep_x_pitched_kernel(Dims d, const double* __restrict__ T, Coeffs c,
+                                                       const uint8_t* __restrict__ vclass,
+                                                       const double* __restrict__ qdense,
+                                                       const double* __restrict__ qshape, QTable qt,
+                                                       double* __restrict__ W0, int64_t line_begin,
+                                                       int64_t line_end) {
+  sweep_x_body<HAS_Q, RANGED, LINES, true>(d, T, c, vclass, qdense, qshape, qt, W0, line_begin, line_end);
 }
 
 // y lines: W1 = s2 * dT1 from W0 = sigma * dT0
 __global__ void __launch_bounds__(kLineThreads) sweep_y_kernel(Dims d, const double* __restrict__ W0,
                                                                 const double* __restrict__ a1,
                                                                 const double* __restrict__ b1,
-                                                                double* __restrict__ W1) {
+                                                                double* __restrict__ W1, int64_t px) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= d.nz * d.nx) return;
   const int64_t k = t / d.nx, i = t - k * d.nx;
-  int64_t p = k * d.nxy() + i;
+  int64_t p = k * d.ny * px + i;  // the y-sweep arrays have row pitch px
   double z = 0.0;
 #pragma unroll 4
-  for (int64_t j = 0; j < d.ny; ++j, p += d.nx) {
+  for (int64_t j = 0; j < d.ny; ++j, p += px) {
     z = fma(-a1[p], z, W0[p]);
     W1[p] = z;
   }
   double x = 0.0;
 #pragma unroll 4
   for (int64_t j = d.ny - 1; j >= 0; --j) {
-    p -= d.nx;
+    p -= px;
     x = fma(-b1[p], x, W1[p]);
     W1[p] = x;
   }
@@ -202,17 +244,21 @@ __global__ void __launch_bounds__(kLineThreads) sweep_z_kernel(Dims d, const dou
                                                                 const double* __restrict__ a2,
                                                                 const double* __restrict__ b2, const double* T_in,
                                                                 double* __restrict__ Z, double* T_out,
-                                                                int64_t col_begin, int64_t col_end) {
-  // this launch covers the z-lines (columns j*nx + i) [col_begin, col_end)
+                                                                int64_t col_begin, int64_t col_end, int64_t px) {
+  // this launch covers the z-lines (columns j*nx + i) [col_begin, col_end); W1 has row pitch px
   const int64_t t = col_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nxy = d.nxy();
   if (t >= col_end) return;
   int64_t p = t;
+  const int64_t jw = t / d.nx;
+  int64_t pw = jw * px + (t - jw * d.nx);
+  const int64_t nxyw = d.ny * px;
+  const uint64_t keep = l2_policy_last();  // the forward values come back to this thread after its last row
   double z = 0.0;
 #pragma unroll 4
-  for (int64_t k = 0; k < d.nz; ++k, p += nxy) {
-    z = fma(-a2[p], z, W1[p]);
-    Z[p] = z;
+  for (int64_t k = 0; k < d.nz; ++k, p += nxy, pw += nxyw) {
+    z = fma(-a2[p], z, W1[pw]);
+    st_keep(Z + p, z, keep);
   }
   double x = 0.0;
 #pragma unroll 4
@@ -298,23 +344,30 @@ cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable&
   const bool has_q = a.has_qtab || a.qdense != nullptr;
   const unsigned gx = blocks(d.nz * d.ny, kXLines);
   if (ev) cudaEventRecord(ev[0], s);
-  if (has_q)
-    sweep_x_kernel<true, false><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0, 0, 0);
+  const bool pitched = c.px != d.nx;
+#define HS2G_X_LAUNCH(KERNEL, ...) \
+  KERNEL<__VA_ARGS__><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, a.qshape, q, a.W0, 0, 0)
+  if (pitched && has_q)
+    HS2G_X_LAUNCH(sweep_x_pitched_kernel, true, false);
+  else if (pitched)
+    HS2G_X_LAUNCH(sweep_x_pitched_kernel, false, false);
+  else if (has_q)
+    HS2G_X_LAUNCH(sweep_x_kernel, true, false);
   else
-    sweep_x_kernel<false, false><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0, 0, 0);
+    HS2G_X_LAUNCH(sweep_x_kernel, false, false);
+#undef HS2G_X_LAUNCH
   if (ev) cudaEventRecord(ev[1], s);
   cudaError_t e = cudaSuccess;
   if (a.bulk_y)
-    e = launch_lines_bulk(d, 1, a.W0, c.a1, a.W1, c.b1, nullptr, a.W1, a.status, a.tmaps, s);
+    e = launch_lines_bulk(d, 1, a.W0, c.a1, a.W1, c.b1, nullptr, a.W1, a.status, a.tmaps, s, c.px);
   else
-    sweep_y_kernel<<<blocks(d.nz * d.nx, kLineThreads), kLineThreads, 0, s>>>(d, a.W0, c.a1, c.b1, a.W1);
+    sweep_y_kernel<<<blocks(d.nz * d.nx, kLineThreads), kLineThreads, 0, s>>>(d, a.W0, c.a1, c.b1, a.W1, c.px);
   if (e != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[2], s);
   if (a.bulk_z)
-    e = launch_lines_bulk(d, 2, a.W1, c.a2, a.W0, c.b2, a.T_in, a.T_out, a.status, a.tmaps, s);
+    e = launch_lines_bulk(d, 2, a.W1, c.a2, a.W0, c.b2, a.T_in, a.T_out, a.status, a.tmaps, s, d.nx);
   else
-    sweep_z_kernel<<<blocks(d.nxy(), kLineThreads), kLineThreads, 0, s>>>(d, a.W1, c.a2, c.b2, a.T_in, a.W0,
-                                                                           a.T_out, 0, d.nxy());
+    e = launch_z_range(a, c, 0, d.nxy(), s);
   if (e != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[3], s);
   return cudaGetLastError();
@@ -329,12 +382,20 @@ void launch_x_lines(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t
                     cudaStream_t s) {
   const Dims& d = a.d;
   const unsigned gx = blocks(line_end - line_begin, LINES);
-  if (a.has_qtab || a.qdense != nullptr)
-    sweep_x_kernel<true, true, LINES><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0,
-                                                               line_begin, line_end);
+  const bool has_q = a.has_qtab || a.qdense != nullptr;
+  const bool pitched = c.px != d.nx;
+#define HS2G_X_LAUNCH(KERNEL, ...) \
+  KERNEL<__VA_ARGS__><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, a.qshape, q, a.W0, line_begin, \
+                                               line_end)
+  if (pitched && has_q)
+    HS2G_X_LAUNCH(sweep_x_pitched_kernel, true, true, LINES);
+  else if (pitched)
+    HS2G_X_LAUNCH(sweep_x_pitched_kernel, false, true, LINES);
+  else if (has_q)
+    HS2G_X_LAUNCH(sweep_x_kernel, true, true, LINES);
   else
-    sweep_x_kernel<false, true, LINES><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, q, a.W0,
-                                                                line_begin, line_end);
+    HS2G_X_LAUNCH(sweep_x_kernel, false, true, LINES);
+#undef HS2G_X_LAUNCH
 }
 
 cudaError_t launch_x_range(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_begin,
@@ -351,8 +412,9 @@ cudaError_t launch_x_range(const StepArgs& a, const Coeffs& c, const QTable& q, 
 
 cudaError_t launch_y(const StepArgs& a, const Coeffs& c, cudaStream_t s) {
   const Dims& d = a.d;
-  if (a.bulk_y) return launch_lines_bulk(d, 1, a.W0, c.a1, a.W1, c.b1, nullptr, a.W1, a.status, a.tmaps, s);
-  sweep_y_kernel<<<blocks(d.nz * d.nx, kLineThreads), kLineThreads, 0, s>>>(d, a.W0, c.a1, c.b1, a.W1);
+  if (a.bulk_y)
+    return launch_lines_bulk(d, 1, a.W0, c.a1, a.W1, c.b1, nullptr, a.W1, a.status, a.tmaps, s, c.px);
+  sweep_y_kernel<<<blocks(d.nz * d.nx, kLineThreads), kLineThreads, 0, s>>>(d, a.W0, c.a1, c.b1, a.W1, c.px);
   return cudaGetLastError();
 }
 
@@ -360,7 +422,8 @@ cudaError_t launch_z_range(const StepArgs& a, const Coeffs& c, int64_t col_begin
   const Dims& d = a.d;
   if (col_end <= col_begin) return cudaSuccess;
   sweep_z_kernel<<<blocks(col_end - col_begin, kLineThreads), kLineThreads, 0, s>>>(d, a.W1, c.a2, c.b2, a.T_in,
-                                                                                   a.W0, a.T_out, col_begin, col_end);
+                                                                                     a.W0, a.T_out, col_begin,
+                                                                                     col_end, c.px);
   return cudaGetLastError();
 }
 

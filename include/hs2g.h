@@ -41,6 +41,8 @@ extern "C" {
 /* flags */
 #define HS2G_DEVICE 1            /* T_in / T_out / qdense / history are device pointers (no copies) */
 #define HS2G_SYNC 2              /* synchronise the handle's stream before returning */
+#define HS2G_REUSE 4             /* hs2g_source_*: use the device copy of the per-voxel array kept from the
+                                    previous call for the same class (the caller's array is unchanged) */
 
 /* material kinds (heatsim2/__init__.py:42-43) */
 #define HS2G_TEMPERATURE_COMPUTE 0
@@ -51,6 +53,10 @@ extern "C" {
 #define HS2G_IMPULSE_SOURCE 1
 #define HS2G_STEPPED_SOURCE 2
 #define HS2G_IMPULSE_POINT_SOURCE_JOULES 3
+/* a class whose per-voxel values come from the handle's source shape (hs2g_source_zdecay, hs2g_source_point):
+   hs2g_source_table gives it 1 at t == params[0] exactly and 0 otherwise (no kind of this number in the
+   reference, whose numpy loop evaluates these sources on every call, alternatingdirection_c_pyx.pyx:307-384) */
+#define HS2G_SHAPED_IMPULSE 5
 
 /*
  * A face flux coefficient as an affine form in the conductivity entries of the two materials that meet at the
@@ -205,6 +211,33 @@ int hs2g_source_table(int nsrc, const int32_t* kind, const double* params, doubl
                       double* qtab);
 
 /*
+ * Per-voxel source shapes: the source kinds whose value differs between the voxels of a class are evaluated on
+ * the device into a per-voxel multiplier S of the handle (1 for every voxel not given a shape).  On every step
+ * the x sweep adds table[class] * S to each voxel's source, so a class given a shape and a table value of 1 on
+ * its firing step (HS2G_SHAPED_IMPULSE) receives exactly the shape's values, and class-uniform sources are
+ * unchanged.  A shape is written for the voxels of its class in the handle's current source-class map; a new
+ * map (hs2g_set_source_classes, or hs2g_step's volumetric argument) resets S to 1 and drops every shape.
+ * Arrays are host pointers (copied into a device buffer of the handle kept per class), device pointers
+ * (HS2G_DEVICE, used in place and needed only until the call's work has run), or, with HS2G_REUSE, the device
+ * copy kept from the previous call for the class.  Work is queued on the handle's stream.
+ */
+/* Replace the source-class map (nz, ny, nx) on the device (host, or device with HS2G_DEVICE). */
+int hs2g_set_source_classes(hs2g_handle* h, const uint8_t* volumetric, int flags);
+/* Spatially z-decaying impulse of class cls (alternatingdirection_c_pyx.pyx:320-384): zgrid (nz, ny, nx) holds
+   each cell's z coordinate; with d = zgrid * direction - offset (direction +1 or -1, the reference's +z or -z
+   unit vector) the cell between d - ddz/2 and d + ddz/2 (clipped at 0) receives the share
+   exp(-a / length) - exp(-b / length) of joules_per_m2, divided by ddz * dt (W/m^3); cells with
+   d + ddz/2 <= 0 receive nothing. */
+int hs2g_source_zdecay(hs2g_handle* h, int cls, const double* zgrid, double direction, double offset, double ddz,
+                       double joules_per_m2, double length, double dt, int flags);
+/* Point-joules impulse of class cls (alternatingdirection_c_pyx.pyx:307-319): joules per cell / (V * dt), the
+   joules one value for every cell (count == 1) or one per cell of the class in C order (count = the class's
+   voxel count), V the cell volume `volume` or, with volumes != NULL, each cell's own (nz, ny, nx) volume (the
+   curved-surface mode). */
+int hs2g_source_point(hs2g_handle* h, int cls, const double* joules, int64_t count, const double* volumes,
+                      double volume, double dt, int flags);
+
+/*
  * One timestep that allocates nothing: no counterpart in the reference.
  *
  * For callers that cannot allocate device memory -- a plugin whose host application owns every device
@@ -265,10 +298,11 @@ int hs2g_batch_autotune(hs2g_batch* b, char* report, int report_len);
  *     J_i = sum_{n < nsteps} sum_{y,x} (T_{n+1}[0, y, x] - obs_i[n, y, x])^2
  * with respect to per-voxel conductivity k (W/m/K), volumetric heat capacity C = rho*c (J/m^3/K), source
  * amplitude q (W/m^3, applied at step n as schedule[n] * q) and the initial temperature, for n instances of
- * uneven size in one concatenated state (a single problem is n = 1).  Each instance is a fully computed box,
- * insulating outside, its interior faces conducting with the arithmetic face mean of boundary_conducting
- * (boundary_conducting.py:7-71); the step is the same Douglas delta form as hs2g_step.  k must be >= 0 and
- * C > 0.  The forward pass checkpoints T every `ckpt` steps; the backward pass recomputes one segment at a
+ * uneven size in one concatenated state (a single problem is n = 1).  Each instance is a box insulating
+ * outside, its interior faces conducting with the arithmetic face mean of boundary_conducting
+ * (boundary_conducting.py:7-71) unless hs2g_adjoint_set_faces gives face classes (insulating, thin-layer and
+ * any other affine scalar-k form) and fixed voxels; the step is the same Douglas delta form as hs2g_step.
+ * k must be >= 0 and C > 0.  The forward pass checkpoints T every `ckpt` steps; the backward pass recomputes one segment at a
  * time from its checkpoint and runs the transposed tridiagonal solves in reverse order (z, y, x).  Every
  * kernel of a sweep covers all instances in one launch.
  */
@@ -291,6 +325,18 @@ int hs2g_adjoint_set_parameters(hs2g_adjoint* a, const double* k, const double* 
    elapsed_ms (or NULL) the device time of the steps. */
 int hs2g_adjoint_forward(hs2g_adjoint* a, int nsteps, const double* schedule, const double* T0, const double* obs,
                          int ckpt, double* loss, double* T_out, int flags, double* elapsed_ms);
+/* Face classes and fixed-temperature voxels, in place of the default (every interior face conducting with the
+   arithmetic mean of k, every voxel computed).  forms[i][c][a][0..2] = (f0, flo, fhi): a face of class c on
+   axis a (0 = z, 1 = y, 2 = x) of instance i conducts f0 + flo * k_lo + fhi * k_hi (W/m^3/K), k_lo and k_hi the
+   conductivities of the voxels below and above it, a fixed voxel's replaced by its computed neighbour's
+   (crank_nicolson.pyx:298-338): the affine form a boundary class has for scalar k (conducting: flo = fhi =
+   1 / (2 d^2); insulating: 0; thin insulating layer: f0 = h / d).  face_z, face_y, face_x (offsets[n] bytes,
+   host or device per flags): the class of each voxel's low face on that axis (ignored on the first layer, the
+   exterior).  fixed (offsets[n] bytes, or NULL): 1 marks a fixed-temperature voxel, which keeps its
+   temperature and whose k, C and q get no gradient.  nclass = 0 (arrays NULL) restores the default.  Applies
+   from the next hs2g_adjoint_set_parameters. */
+int hs2g_adjoint_set_faces(hs2g_adjoint* a, int nclass, const double* forms, const uint8_t* face_z,
+                           const uint8_t* face_y, const uint8_t* face_x, const uint8_t* fixed, int flags);
 /* dJ_i/dk, dJ_i/dC, dJ_i/dq and (gT0 not NULL) dJ_i/dT0 of the last forward pass, offsets[n] doubles each. */
 int hs2g_adjoint_backward(hs2g_adjoint* a, double* gk, double* gC, double* gq, double* gT0, int flags,
                           double* elapsed_ms);

@@ -22,6 +22,30 @@ def low_faces(k, spacing):
     return gz, gy, gx
 
 
+FIXED_CAPACITY = 1e300   # kFixedCapacity of hs2g_adjoint.cu
+
+
+def low_faces_general(k, forms, low, fixed):
+    """Low-face conductances with face classes and fixed voxels, as adj_setup_faces_kernel: the class's form
+    f0 + flo k_lo + fhi k_hi, a fixed side's k replaced by its neighbour's, 0 between two fixed voxels."""
+    out = []
+    for a in range(3):
+        g = np.zeros_like(k)
+        lo = [slice(None)] * 3
+        hi = [slice(None)] * 3
+        lo[a] = slice(None, -1)
+        hi[a] = slice(1, None)
+        lo, hi = tuple(lo), tuple(hi)
+        flo, fhi = fixed[lo], fixed[hi]
+        klo = np.where(flo, k[hi], k[lo])
+        khi = np.where(fhi, k[lo], k[hi])
+        c = forms[low[a][hi].astype(np.int64), a]
+        G = c[..., 0] + c[..., 1] * klo + c[..., 2] * khi
+        g[hi] = np.where(flo & fhi, 0.0, G)
+        out.append(g)
+    return tuple(out)
+
+
 def factor(M, g, axis):
     """(e, u, ip) of M - L_axis/2 along `axis`, as adj_factor_kernel: e = lo / piv, u = super / piv, ip = 1/piv."""
     Mt = np.moveaxis(M, axis, -1)
@@ -97,11 +121,15 @@ def diagonal(gz, gy, gx):
 
 
 class Model(object):
-    def __init__(self, k, C, q, dt, spacing):
+    """forms / low / fixed: face classes and fixed voxels (hs2g_adjoint_set_faces), else every face conducts."""
+
+    def __init__(self, k, C, q, dt, spacing, forms=None, low=None, fixed=None):
         self.k, self.C, self.q, self.dt, self.spacing = k, C, q, dt, spacing
-        self.g = low_faces(k, spacing)
+        self.forms, self.low = forms, low
+        self.fixed = np.zeros(k.shape, dtype=bool) if fixed is None else np.asarray(fixed, dtype=bool)
+        self.g = low_faces(k, spacing) if forms is None else low_faces_general(k, forms, low, self.fixed)
         self.D = diagonal(*self.g)
-        self.M = C * (1.0 / dt)
+        self.M = np.where(self.fixed, FIXED_CAPACITY, C * (1.0 / dt))
         gz, gy, gx = self.g
         self.f = [factor(self.M, gx, 2), factor(self.M, gy, 1), factor(self.M, gz, 0)]
 
@@ -159,13 +187,32 @@ class Model(object):
                 gq += self.schedule[s] * mu0
         dz, dy, dx = self.spacing
         gk = np.zeros_like(self.k)
-        for a, (gf, d) in enumerate(zip(gg, (dx, dy, dz))):
-            ax = 2 - a
-            sl_hi = [slice(None)] * 3
-            sl_lo = [slice(None)] * 3
-            sl_hi[ax] = slice(1, None)
-            sl_lo[ax] = slice(None, -1)
-            face = gf[tuple(sl_hi)] * (0.5 / (d * d))
-            gk[tuple(sl_hi)] += face
-            gk[tuple(sl_lo)] += face
-        return gk, gM / self.dt, gq, lam
+        if self.forms is None:
+            for a, (gf, d) in enumerate(zip(gg, (dx, dy, dz))):
+                ax = 2 - a
+                sl_hi = [slice(None)] * 3
+                sl_lo = [slice(None)] * 3
+                sl_hi[ax] = slice(1, None)
+                sl_lo[ax] = slice(None, -1)
+                face = gf[tuple(sl_hi)] * (0.5 / (d * d))
+                gk[tuple(sl_hi)] += face
+                gk[tuple(sl_lo)] += face
+            return gk, gM / self.dt, gq, lam
+        # adj_chain_faces_kernel: each face's gradient times dG/dk of its two sides (both coefficients to the
+        # computed side when the other is fixed); fixed voxels' k, C and q get none
+        fx = self.fixed
+        for ax in range(3):
+            gf = gg[2 - ax]                       # gg holds x, y, z
+            lo = [slice(None)] * 3
+            hi = [slice(None)] * 3
+            lo[ax] = slice(None, -1)
+            hi[ax] = slice(1, None)
+            lo, hi = tuple(lo), tuple(hi)
+            c = self.forms[self.low[ax][hi].astype(np.int64), ax]
+            face = gf[hi]
+            gk[hi] += face * np.where(fx[lo], c[..., 1] + c[..., 2], c[..., 2])
+            gk[lo] += face * np.where(fx[hi], c[..., 1] + c[..., 2], c[..., 1])
+        gk[fx] = 0.0
+        gC = np.where(fx, 0.0, gM / self.dt)
+        gq = np.where(fx, 0.0, gq)
+        return gk, gC, gq, lam

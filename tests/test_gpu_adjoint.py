@@ -60,6 +60,111 @@ def test_gradients_match_autograd(cuda_ok):
         assert rel_err(mine, t.grad.numpy()) <= 1e-10, name
 
 
+def _faces_problem(seed, shape, N, sp=(1e-3, 1.1e-3, 0.9e-3)):
+    """_problem with the forward path's face classes and fixed voxels: a thin insulating layer patch (h = 1000
+    W/m^2/K) and an insulating delamination under the surface, a thin layer across x, an insulating exterior,
+    a fixed-temperature bottom layer and two fixed voxels inside."""
+    import heatsim2_gb300 as hs
+    p = _problem(seed, shape, N, sp)
+    nz, ny, nx = shape
+    bz = np.zeros((nz + 1, ny, nx), np.uint8)
+    by = np.zeros((nz, ny + 1, nx), np.uint8)
+    bx = np.zeros((nz, ny, nx + 1), np.uint8)
+    bz[[0, -1]] = 1
+    by[:, [0, -1]] = 1
+    bx[:, :, [0, -1]] = 1
+    bz[2, 2:ny - 3, 3:nx - 2] = 2
+    bz[4, ny // 2:, 1:nx // 2] = 1
+    bx[1:4, 3:ny - 2, nx // 2] = 2
+    fixed = np.zeros(shape, dtype=bool)
+    fixed[-1] = True
+    fixed[3, 4, 5] = fixed[5, 2, nx - 3] = True
+    bnd = ((hs.boundary_conducting,), (hs.boundary_insulating,), (hs.boundary_thininsulatinglayer, 1000.0))
+    p.update(faces=(bnd, bz, by, bx), fixed=fixed)
+    return p
+
+
+def test_face_class_gradients_match_autograd(cuda_ok):
+    """(8,16,16) FP64, 40 steps, with a thin-layer flaw, an insulating delamination, a thin layer across x and
+    fixed voxels (a fixed bottom layer): the forward states match the PyTorch ADI's class-problem model and every
+    gradient matches autograd through it (fixed voxels' k, rho*c and q get none)."""
+    from heatsim2_gb300.adjoint import face_classes
+    dt, N = 0.01, 40
+    p = _faces_problem(2, (8, 16, 16), N)
+    a = Adjoint([(p["shape"], p["spacing"])], dt)
+    a.set_faces(p["faces"], p["fixed"])
+    a.set_parameters(p["k"], p["C"], p["q"])
+    loss, T = a.forward(p["T0"], p["obs"], p["schedule"], 10, return_state=True)
+    g = a.backward()
+    forms, low = face_classes(p["shape"], p["spacing"], p["faces"], p["fixed"])
+    tk = [torch.tensor(p[n], requires_grad=True) for n in ("k", "C", "q", "T0")]
+    kw = dict(forms=forms, low=low, fixed=p["fixed"])
+    states = TA.run(tk[3], tk[0], tk[1], tk[2], p["schedule"], dt, p["spacing"], **kw)
+    assert rel_err(T, states[-1].detach().numpy()) <= 1e-12
+    np.testing.assert_array_equal(T[p["fixed"]], p["T0"][p["fixed"]])
+    J = TA.misfit(tk[3], tk[0], tk[1], tk[2], p["schedule"], torch.tensor(p["obs"]), dt, p["spacing"], **kw)
+    J.backward()
+    assert abs(loss[0] - J.item()) <= 1e-12 * J.item()
+    for name, mine, t in zip(("k", "C", "q", "T0"), g, tk):
+        assert rel_err(mine, t.grad.numpy()) <= 1e-10, name
+        if name != "T0":
+            assert not mine[p["fixed"]].any(), name
+
+
+def test_face_class_batch_equals_single_instances(cuda_ok):
+    """Face classes and fixed voxels per instance in one batch give each instance's single-handle loss and
+    gradients bit for bit (the forms table is per instance: the spacings differ), and clearing the faces
+    restores the default model bit for bit."""
+    dt, N = 0.005, 10
+    probs = [_faces_problem(20 + i, s, N, sp) for i, (s, sp) in enumerate(
+        [((6, 9, 10), (1e-3, 1e-3, 1e-3)), ((7, 8, 12), (5e-4, 6e-4, 7e-4))])]
+    probs[1]["schedule"] = probs[0]["schedule"]
+    b = Adjoint([(p["shape"], p["spacing"]) for p in probs], dt)
+    b.set_faces([p["faces"] for p in probs], [p["fixed"] for p in probs])
+    b.set_parameters([p["k"] for p in probs], [p["C"] for p in probs], [p["q"] for p in probs])
+    lb = b.forward([p["T0"] for p in probs], [p["obs"] for p in probs], probs[0]["schedule"], 4)
+    gb = b.backward()
+    for i, p in enumerate(probs):
+        a = Adjoint([(p["shape"], p["spacing"])], dt)
+        a.set_faces(p["faces"], p["fixed"])
+        a.set_parameters(p["k"], p["C"], p["q"])
+        la = a.forward(p["T0"], p["obs"], p["schedule"], 4)
+        ga = a.backward()
+        assert lb[i] == la[0]
+        for x, y in zip(gb, ga):
+            np.testing.assert_array_equal(x[i], y)
+        a.set_faces(None)
+        a.set_parameters(p["k"], p["C"], p["q"])
+        lc = a.forward(p["T0"], p["obs"], p["schedule"], 4)
+        fresh, lf = _adjoint(p, dt, 4)
+        assert lc[0] == lf[0]
+        for x, y in zip(a.backward(), fresh.backward()):
+            np.testing.assert_array_equal(x, y)
+
+
+def test_autograd_function_with_faces(cuda_ok):
+    """surface_misfit with face classes and fixed voxels carries the incoming gradient onto the numpy-driven
+    adjoint's gradients; a following call without faces on a pooled handle is the default model again."""
+    dt, N = 0.01, 12
+    p = _faces_problem(5, (6, 8, 9), N)
+    a = Adjoint([(p["shape"], p["spacing"])], dt)
+    a.set_faces(p["faces"], p["fixed"])
+    a.set_parameters(p["k"], p["C"], p["q"])
+    loss = a.forward(p["T0"], p["obs"], p["schedule"], 5)
+    g = a.backward()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    t = {n: torch.tensor(p[n], device=dev, requires_grad=n != "obs") for n in ("k", "C", "q", "T0", "obs")}
+    J = surface_misfit(t["k"], t["C"], t["q"], t["T0"], t["obs"], p["schedule"], p["spacing"], dt, ckpt=5,
+                       faces=p["faces"], fixed=p["fixed"])
+    assert abs(J.item() - loss[0]) <= 1e-13 * loss[0]
+    (2.0 * J).backward()
+    for name, ref in zip(("k", "C", "q", "T0"), g):
+        assert rel_err(t[name].grad.cpu().numpy(), 2.0 * ref) <= 1e-12, name
+    J0 = surface_misfit(t["k"], t["C"], t["q"], t["T0"], t["obs"], p["schedule"], p["spacing"], dt, ckpt=5)
+    fresh, l0 = _adjoint(p, dt, 5)
+    assert abs(J0.item() - l0[0]) <= 1e-13 * l0[0]
+
+
 def test_checkpoint_interval_changes_nothing(cuda_ok):
     dt, N = 0.01, 23
     p = _problem(3, (5, 9, 11), N)
@@ -245,18 +350,21 @@ def test_steel_adjoint_central_differences_64_voxels(cuda_ok):
     """The (32,128,128) steel inverse problem, 500 steps of 10 ms, checkpoint every 50: k, rho*c and q
     gradients at 64 random voxels agree with central differences to 1e-6 relative (floored at 1e-3 of the
     field's largest gradient).  Entries above the floor are judged by their own relative error; how many the
-    floor decided is printed and bounded."""
+    floor decided is printed, and 32 further voxels in the top two layers must all be judged relatively."""
     w = W.adjoint_steel()
     p = dict(k=w["k"], C=w["C"], q=w["q"], T0=w["T0"], schedule=w["schedule"], obs=w["obs"],
              spacing=w["spacing"], shape=w["shape"])
     rng = np.random.default_rng(8)
     vox = [tuple(int(rng.integers(0, n)) for n in w["shape"]) for _ in range(64)]
-    errs = _fd_errors(p, w["dt"], w["ckpt"], vox)
+    # 32 more in the two layers under the observed surface, where every gradient entry stands above the floor
+    top = [(int(rng.integers(0, 2)), int(rng.integers(0, w["shape"][1])), int(rng.integers(0, w["shape"][2])))
+           for _ in range(32)]
+    errs = _fd_errors(p, w["dt"], w["ckpt"], vox + top)
     floored, total = _check_fd(errs, label="steel (32,128,128)")
-    # the floor decides only voxels the surface barely sees; at least half of each field's entries are judged by
-    # their own relative error
-    for name in total:
-        assert floored[name] <= total[name] // 2, floored
+    # uniform voxels over the depth: most lie deeper than the flash reaches in 5 s, and the floor decides those
+    # (counts printed above); the top-layer voxels must all be judged by their own relative error
+    top_floored = [key for key in errs if key[1] in set(top) and errs[key][1]]
+    assert not top_floored, top_floored
 
 
 def test_autograd_function_single(cuda_ok):

@@ -138,18 +138,24 @@ def test_composite_panel_midsize_vs_oracle(cuda_ok):
     _compare_with_oracle(spec, 25)
 
 
-def test_bulk_copy_and_plain_line_sweeps_agree_bitwise(cuda_ok, monkeypatch):
-    """The TMA bulk-copy y/z sweeps (even row widths) and the plain-load sweeps do the same FMAs in the same
-    order, so their results are identical."""
-    spec = W.composite_panel(seed=5, nz=20, ny=70, nx=66, top_layers=6, width_range=(5, 30), depth_range=(2, 15))
+@pytest.mark.parametrize("shape", [(20, 70, 66), (9, 33, 41)])
+def test_sweep_kernel_variants_agree_bitwise(cuda_ok, monkeypatch, shape):
+    """Every selectable sweep kernel does the same FMAs in the same order, so the results are identical: TMA
+    bulk-copy or plain-load y / z sweeps, and the y sweep's arrays unpadded (even nx) or padded to a row pitch
+    of 64 (odd nx always gets one pad column, so that the TMA sweep applies)."""
+    nz, ny, nx = shape
+    spec = W.composite_panel(seed=5, nz=nz, ny=ny, nx=nx, top_layers=4, width_range=(5, 20), depth_range=(2, 6))
     outs = []
-    for y_mode, z_mode in (("tma", "plain"), ("plain", "tma"), ("plain", "plain")):
+    variants = (("tma", "plain", "2"), ("plain", "tma", "2"), ("plain", "plain", "2"), ("tma", "plain", "64"),
+                ("plain", "plain", "64"))
+    for y_mode, z_mode, pitch in variants:
         monkeypatch.setenv("HS2G_LINE_SWEEP", y_mode)
         monkeypatch.setenv("HS2G_Z_SWEEP", z_mode)
+        monkeypatch.setenv("HS2G_ROW_PITCH", pitch)   # rows of the y-sweep arrays padded to this multiple
         P, S = _setup(spec)
         outs.append(_run_host(spec, W.step_times(spec, 5), P, S)[5])
-    np.testing.assert_array_equal(outs[0], outs[1])
-    np.testing.assert_array_equal(outs[0], outs[2])
+    for o in outs[1:]:
+        np.testing.assert_array_equal(outs[0], o)
 
 
 def test_uneven_instances_vs_oracle(cuda_ok):
@@ -287,6 +293,64 @@ def test_dense_source_on_device(cuda_ok):
     for t in times:
         T = hs.run_adi_steps(P, S, t, spec["dt"], T, spec["arrays"]["volumetric"], vol)
     assert rel_err(T.cpu().numpy(), ref[len(times)]) <= TOL
+
+
+def test_per_voxel_sources_on_device_at_full_size(cuda_ok, monkeypatch):
+    """A z-decaying impulse and an array-valued point source on the benchmark grid (65x512x512, class map
+    replaced by the call).  Their values are evaluated on the device (pyx:307-384): a repeat firing step with the
+    same z coordinates uploads nothing but T (the z-coordinate array stays on the device, the shape call is
+    flagged REUSE and no per-voxel field goes up), and the step equals one given the source field as the
+    reference's numpy loop forms it (oracle restatement) within 1e-12."""
+    import ctypes
+    from heatsim2_gb300 import _native
+    spec = W.composite_panel(seed=1)
+    g = spec["grid"]
+    nz, ny, nx = g["nz"], g["ny"], g["nx"]
+    P, S = _setup(spec)
+    vclass = np.zeros((nz, ny, nx), dtype=np.uint8)
+    vclass[1:9] = 1                                     # z-decaying absorption in the top compute layers
+    vclass[20:26, 100:140, 300:330] = 2                 # a buried block with per-voxel point energies
+    zc = (g["z0"] + g["dz"] * np.arange(nz))[:, None, None]
+    zgrid = np.ascontiguousarray(np.broadcast_to(zc, (nz, ny, nx)))
+    rng = np.random.default_rng(17)
+    joules = rng.uniform(1e-4, 1e-3, int((vclass == 2).sum()))
+
+    def vol(jpm2):
+        return ((hs.NO_SOURCE,),
+                (hs.SPATIALLY_Z_DECAYING_TEMPORAL_IMPULSE, 0.0, np.array([1.0, 0.0, 0.0]), g["z0"] + 0.5 * g["dz"],
+                 zgrid, g["dz"], jpm2, 1.5e-3),
+                (hs.IMPULSE_POINT_SOURCE_JOULES, 0.0, joules))
+
+    L = _native.load()
+    calls = []
+    for name in ("hs2g_source_zdecay", "hs2g_source_point", "hs2g_set_source_classes", "hs2g_step"):
+        fn = getattr(L, name)
+
+        def spy(*args, _fn=fn, _name=name):
+            calls.append((_name, args))
+            return _fn(*args)
+        monkeypatch.setattr(L, name, spy)
+    T0 = W.initial_temperature(spec)
+    first = hs.run_adi_steps(P, S, 0.0, spec["dt"], T0, vclass, vol(2e4))
+    assert {c[0] for c in calls} >= {"hs2g_source_zdecay", "hs2g_source_point", "hs2g_set_source_classes"}
+    calls.clear()
+    second_vol = vol(3e4)                               # new amplitude, same z coordinates and joules
+    second = hs.run_adi_steps(P, S, 0.0, spec["dt"], T0, vclass, second_vol)
+    names = [c[0] for c in calls]
+    assert "hs2g_set_source_classes" not in names       # the class map is already on the device
+    assert "hs2g_source_point" not in names             # unchanged source: its shape is kept
+    (zcall,) = [c for c in calls if c[0] == "hs2g_source_zdecay"]
+    assert zcall[1][-1] & _native.REUSE                 # z coordinates reused from the device copy
+    (step,) = [c for c in calls if c[0] == "hs2g_step"]
+    assert step[1][4] is None and step[1][5] is None    # no per-voxel source field, no class map uploaded
+    # the same step with the reference-form source field handed over explicitly
+    from oracle_shim import HS
+    Q = oracle.source_field(P.shape, P.volume_array, 0.0, spec["dt"], vclass, second_vol)
+    assert Q[1].max() > 0 and Q[vclass == 2].min() > 0
+    ref = np.empty_like(T0)
+    _native.check(L.hs2g_step(P.handle.ptr, T0.ctypes.data, ref.ctypes.data, None, Q.ctypes.data, None, 0))
+    assert rel_err(second, ref) <= TOL, rel_err(second, ref)
+    assert np.abs(first - T0).max() > 0.1 and np.abs(second - first).max() > 0.01
 
 
 # ---- errors where the reference errors (or silently computes outside the domain) ----------------------

@@ -85,19 +85,13 @@ def test_static_step_rejects_grids_beyond_the_maximum(cuda_ok):
 
 
 def _source_field(spec, P, t):
-    """The per-voxel source (W/m^3) of a fixture at time t: class-uniform values scattered by the class map,
-    plus the per-voxel kinds."""
-    from heatsim2_gb300.alternatingdirection import _ClassSources, _dense_source, source_table
-    vol = W.volumetric_tuple(hs, spec)
-    src = _ClassSources(vol)
-    q, _ = source_table(src, t, spec["dt"], P.volume_array)
-    vclass = np.asarray(spec["arrays"]["volumetric"])
-    Q = q[vclass]
-    if src.dense:
-        qd = _dense_source(P.shape, P.volume_array, t, spec["dt"], vclass, src.dense)
-        if qd is not None:
-            Q = Q + qd
-    return np.ascontiguousarray(Q)
+    """The per-voxel source (W/m^3) of a fixture at time t, as the reference's numpy loop forms it (the
+    oracle's restatement of alternatingdirection_c_pyx.pyx:294-386)."""
+    import oracle
+    from oracle_shim import HS
+    return np.ascontiguousarray(oracle.source_field(P.shape, P.volume_array, t, spec["dt"],
+                                                    np.asarray(spec["arrays"]["volumetric"]),
+                                                    W.volumetric_tuple(HS, spec)))
 
 
 @pytest.mark.parametrize("name", ["mixed_small", "sources_small", "steel_slab"])
