@@ -17,6 +17,8 @@
 //   z sweep: one thread per z-line (j,i); neighbouring lanes have neighbouring i, so each k step is one
 //            coalesced 256-byte access per array per warp (a TMA variant exists, HS2G_Z_SWEEP=tma).
 #include <cmath>
+#include <cstdlib>
+#include <cstring>
 
 #include "hs2g_internal.cuh"
 
@@ -52,12 +54,25 @@ __device__ __forceinline__ uint64_t l2_policy_last() {
 __device__ __forceinline__ void st_keep(double* p, double v, uint64_t policy) {
   asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(v), "l"(policy) : "memory");
 }
+__device__ __forceinline__ uint64_t l2_policy_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+// a read-only load carrying an L2 policy (evict-first: streamed data that should not displace the round trip)
+template <bool HINT>
+__device__ __forceinline__ double ldc(const double* p, uint64_t policy) {
+  if (!HINT) return *p;
+  double v;
+  asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(policy));
+  return v;
+}
 
-template <bool HAS_Q>
+template <bool HAS_Q, bool HINT = false>
 __device__ __forceinline__ double stencil_x(const Dims& d, const double* __restrict__ T, const Coeffs& c,
                                             const uint8_t* __restrict__ vclass, const double* __restrict__ qdense,
                                             const double* __restrict__ qshape, const double* sq, int64_t L, int ch,
-                                            int lane) {
+                                            int lane, uint64_t first = 0) {
   const int64_t i = (int64_t)ch * 32 + lane;
   const int64_t k = L / d.ny, j = L - k * d.ny;
   const int64_t p = L * d.nx + i;
@@ -70,13 +85,13 @@ __device__ __forceinline__ double stencil_x(const Dims& d, const double* __restr
   const double tyh = j + 1 < d.ny ? T[p + d.nx] : t;
   const double tzl = k > 0 ? T[p - nxy] : t;
   const double tzh = k + 1 < d.nz ? T[p + nxy] : t;
-  double r = w[kWc * 32] * t;
-  r = fma(w[kWxl * 32], txl, r);
-  r = fma(w[kWxh * 32], txh, r);
-  r = fma(w[kWyl * 32], tyl, r);
-  r = fma(w[kWyh * 32], tyh, r);
-  r = fma(w[kWzl * 32], tzl, r);
-  r = fma(w[kWzh * 32], tzh, r);
+  double r = ldc<HINT>(w + kWc * 32, first) * t;
+  r = fma(ldc<HINT>(w + kWxl * 32, first), txl, r);
+  r = fma(ldc<HINT>(w + kWxh * 32, first), txh, r);
+  r = fma(ldc<HINT>(w + kWyl * 32, first), tyl, r);
+  r = fma(ldc<HINT>(w + kWyh * 32, first), tyh, r);
+  r = fma(ldc<HINT>(w + kWzl * 32, first), tzl, r);
+  r = fma(ldc<HINT>(w + kWzh * 32, first), tzh, r);
   if (HAS_Q) {
     double q = sq[vclass[p]];
     if (qshape) q *= qshape[p];
@@ -91,13 +106,16 @@ __device__ __forceinline__ double stencil_x(const Dims& d, const double* __restr
 // its own register allocation.  LINES x-lines per CTA: 32 for the whole grid; the host-buffer step's later,
 // smaller slabs take 16 or 8, whose CTAs finish sooner (a CTA's chunk loop, not the GPU's throughput, sets
 // how long a small launch takes).
-// PITCHED: W0 rows have the pitch c.px (padded: odd nx, or padding for tests); otherwise W0 shares T's pitch nx.
-template <bool PITCHED>
+// PITCH 0: W0 shares T's row pitch nx; 1: one pad column (odd nx: pitch nx + 1, so the W0 index of voxel (L, i)
+// is its T index plus L); 2: any other pitch c.px (padding for tests).
+template <int PITCH>
 __device__ __forceinline__ int64_t w0_index(const Dims& d, const Coeffs& c, int64_t L, int64_t i) {
-  return PITCHED ? L * c.px + i : L * d.nx + i;
+  if (PITCH == 0) return L * d.nx + i;
+  if (PITCH == 1) return L * d.nx + i + L;
+  return L * c.px + i;
 }
 
-template <bool HAS_Q, bool RANGED, int LINES, bool PITCHED>
+template <bool HAS_Q, bool RANGED, int LINES, int PITCHED, bool HINT = false>
 __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __restrict__ T, const Coeffs& c,
                                              const uint8_t* __restrict__ vclass, const double* __restrict__ qdense,
                                              const double* __restrict__ qshape, const QTable& qt,
@@ -113,6 +131,7 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
   const int64_t nlines = RANGED ? line_end : d.nz * d.ny;
   const int64_t L0 = (RANGED ? line_begin : 0) + (int64_t)blockIdx.x * LINES;
   const int nchunks = (int)((d.nx + kXChunk - 1) / kXChunk);
+  const uint64_t first = HINT ? l2_policy_first() : 0, keep = HINT ? l2_policy_last() : 0;
   __syncthreads();
 
   // forward: z_i = R'_i - a0_i * z_{i-1}
@@ -125,8 +144,8 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
       const int64_t L = L0 + l;
       double r = 0.0, a = 0.0;
       if (L < nlines && i < d.nx) {
-        r = stencil_x<HAS_Q>(d, T, c, vclass, qdense, qshape, sq, L, ch, lane);
-        a = c.a0[L * d.nx + i];
+        r = stencil_x<HAS_Q, HINT>(d, T, c, vclass, qdense, qshape, sq, L, ch, lane, first);
+        a = ldc<HINT>(c.a0 + L * d.nx + i, first);
       }
       sr[l][lane] = r;
       sa[l][lane] = a;
@@ -147,7 +166,12 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
     for (int ll = 0; ll < kPerWarp; ++ll) {
       const int l = warp * kPerWarp + ll;
       const int64_t L = L0 + l;
-      if (L < nlines && i < d.nx) W0[w0_index<PITCHED>(d, c, L, i)] = sr[l][lane];
+      if (L < nlines && i < d.nx) {
+        if (HINT)
+          st_keep(W0 + w0_index<PITCHED>(d, c, L, i), sr[l][lane], keep);
+        else
+          W0[w0_index<PITCHED>(d, c, L, i)] = sr[l][lane];
+      }
     }
     __syncthreads();
   }
@@ -164,7 +188,7 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
       if (L < nlines && i < d.nx) {
         const int64_t p = L * d.nx + i;
         z = W0[w0_index<PITCHED>(d, c, L, i)];
-        b = c.b0[p];
+        b = ldc<HINT>(c.b0 + p, first);
       }
       sr[l][lane] = z;
       sa[l][lane] = b;
@@ -191,7 +215,8 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
   }
 }
 
-// The whole-grid and ranged x sweeps with W0 rows unpadded (even nx): 72 registers with a bound of 6 blocks.
+// The x sweep of almost every step (no source term, W0 rows unpadded): 72 registers under a bound of 6 blocks,
+// its fastest schedule (334 us at 65x512x512).  Also the line-range instances of the host-buffer step.
 template <bool HAS_Q, bool RANGED, int LINES = kXLines>
 __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d, const double* __restrict__ T, Coeffs c,
                                                              const uint8_t* __restrict__ vclass,
@@ -199,19 +224,59 @@ __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d,
                                                              const double* __restrict__ qshape, QTable qt,
                                                              double* __restrict__ W0, int64_t line_begin,
                                                              int64_t line_end) {
-  sweep_x_body<HAS_Q, RANGED, LINES, false>(d, T, c, vclass, qdense, qshape, qt, W0, line_begin, line_end);
+  sweep_x_body<HAS_Q, RANGED, LINES, 0>(d, T, c, vclass, qdense, qshape, qt, W0, line_begin, line_end);
 }
-// The same with padded W0 rows (odd nx): the separate row index costs registers (80 under the bound of 6
-// blocks, which puts the grid into two waves), so the budget is set directly to the 72 that keep 7 CTAs per SM
-// (365 us at 65x512x511 against 338 us for the unpadded kernel at 65x512x512).
-template <bool HAS_Q, bool RANGED, int LINES = kXLines>
-__global__ void __maxnreg__(72) sweep_x_pitched_kernel(Dims d, const double* __restrict__ T, Coeffs c,
-                                                       const uint8_t* __restrict__ vclass,
-                                                       const double* __restrict__ qdense,
-                                                       const double* __restrict__ qshape, QTable qt,
-                                                       double* __restrict__ W0, int64_t line_begin,
-                                                       int64_t line_end) {
-  sweep_x_body<HAS_Q, RANGED, LINES, true>(d, T, c, vclass, qdense, qshape, qt, W0, line_begin, line_end);
+// The whole-grid sweep with a source term or with padded W0 rows: under the 6-block bound these take 78-80
+// registers, 6 CTAs per SM, so the 1040 CTAs of a 65x512-line grid run in two waves (694 us for a source step);
+// their register budget is set directly to the 72 that keep 7 CTAs per SM (padded rows of an odd nx with the
+// one-column index: 349 us at 65x512x511; with a general pitch: 362 us).
+template <bool HAS_Q, bool RANGED, int LINES, int PITCH, bool HINT = false>
+__global__ void __maxnreg__(72) sweep_x_lean_kernel(Dims d, const double* __restrict__ T, Coeffs c,
+                                                    const uint8_t* __restrict__ vclass,
+                                                    const double* __restrict__ qdense,
+                                                    const double* __restrict__ qshape, QTable qt,
+                                                    double* __restrict__ W0, int64_t line_begin, int64_t line_end) {
+  sweep_x_body<HAS_Q, RANGED, LINES, PITCH, HINT>(d, T, c, vclass, qdense, qshape, qt, W0, line_begin, line_end);
+}
+
+// x sweep over all lines (RANGED false) or the lines [line_begin, line_end) of the host-buffer step
+template <bool RANGED, int LINES>
+void launch_x(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_begin, int64_t line_end,
+              cudaStream_t s) {
+  const Dims& d = a.d;
+  const unsigned gx = (unsigned)(((RANGED ? line_end - line_begin : d.nz * d.ny) + LINES - 1) / LINES);
+  const bool has_q = a.has_qtab || a.qdense != nullptr;
+  const int pitch = c.px == d.nx ? 0 : c.px == d.nx + 1 ? 1 : 2;
+#define HS2G_X(KERNEL, ...) \
+  KERNEL<__VA_ARGS__><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, a.qshape, q, a.W0, line_begin, \
+                                               line_end)
+  const char* xv = getenv("HS2G_X_VARIANT");
+  if (!RANGED && pitch == 0 && !has_q && xv && strcmp(xv, "lean") == 0) {
+    HS2G_X(sweep_x_lean_kernel, false, false, LINES, 0, false);
+  } else if (!RANGED && pitch == 0 && !has_q && xv && strcmp(xv, "lean_hint") == 0) {
+    HS2G_X(sweep_x_lean_kernel, false, false, LINES, 0, true);
+  } else if (pitch == 0 && (!has_q || RANGED)) {
+    if (has_q)
+      HS2G_X(sweep_x_kernel, true, RANGED, LINES);
+    else
+      HS2G_X(sweep_x_kernel, false, RANGED, LINES);
+  } else if (pitch == 0) {
+    if (has_q)
+      HS2G_X(sweep_x_lean_kernel, true, RANGED, LINES, 0);
+    else
+      HS2G_X(sweep_x_lean_kernel, false, RANGED, LINES, 0);
+  } else if (pitch == 1) {
+    if (has_q)
+      HS2G_X(sweep_x_lean_kernel, true, RANGED, LINES, 1);
+    else
+      HS2G_X(sweep_x_lean_kernel, false, RANGED, LINES, 1);
+  } else {
+    if (has_q)
+      HS2G_X(sweep_x_lean_kernel, true, RANGED, LINES, 2);
+    else
+      HS2G_X(sweep_x_lean_kernel, false, RANGED, LINES, 2);
+  }
+#undef HS2G_X
 }
 
 // y lines: W1 = s2 * dT1 from W0 = sigma * dT0
@@ -341,21 +406,8 @@ cudaError_t fp64_fma_rate(double* fma_per_s) {
 cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s,
                                cudaEvent_t ev[4]) {
   const Dims& d = a.d;
-  const bool has_q = a.has_qtab || a.qdense != nullptr;
-  const unsigned gx = blocks(d.nz * d.ny, kXLines);
   if (ev) cudaEventRecord(ev[0], s);
-  const bool pitched = c.px != d.nx;
-#define HS2G_X_LAUNCH(KERNEL, ...) \
-  KERNEL<__VA_ARGS__><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, a.qshape, q, a.W0, 0, 0)
-  if (pitched && has_q)
-    HS2G_X_LAUNCH(sweep_x_pitched_kernel, true, false);
-  else if (pitched)
-    HS2G_X_LAUNCH(sweep_x_pitched_kernel, false, false);
-  else if (has_q)
-    HS2G_X_LAUNCH(sweep_x_kernel, true, false);
-  else
-    HS2G_X_LAUNCH(sweep_x_kernel, false, false);
-#undef HS2G_X_LAUNCH
+  launch_x<false, kXLines>(a, c, q, 0, 0, s);
   if (ev) cudaEventRecord(ev[1], s);
   cudaError_t e = cudaSuccess;
   if (a.bulk_y)
@@ -380,22 +432,7 @@ cudaError_t launch_step(const StepArgs& a, const Coeffs& c, const QTable& q, cud
 template <int LINES>
 void launch_x_lines(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_begin, int64_t line_end,
                     cudaStream_t s) {
-  const Dims& d = a.d;
-  const unsigned gx = blocks(line_end - line_begin, LINES);
-  const bool has_q = a.has_qtab || a.qdense != nullptr;
-  const bool pitched = c.px != d.nx;
-#define HS2G_X_LAUNCH(KERNEL, ...) \
-  KERNEL<__VA_ARGS__><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, a.qshape, q, a.W0, line_begin, \
-                                               line_end)
-  if (pitched && has_q)
-    HS2G_X_LAUNCH(sweep_x_pitched_kernel, true, true, LINES);
-  else if (pitched)
-    HS2G_X_LAUNCH(sweep_x_pitched_kernel, false, true, LINES);
-  else if (has_q)
-    HS2G_X_LAUNCH(sweep_x_kernel, true, true, LINES);
-  else
-    HS2G_X_LAUNCH(sweep_x_kernel, false, true, LINES);
-#undef HS2G_X_LAUNCH
+  launch_x<true, LINES>(a, c, q, line_begin, line_end, s);
 }
 
 cudaError_t launch_x_range(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_begin,
