@@ -31,11 +31,11 @@ constexpr int kXThreads = 128;
 constexpr int kXWarps = kXThreads / 32;
 constexpr int kXLinesPerWarp = kXLines / kXWarps;
 // Register budget of the x sweep: at 72 registers 7 CTAs of 128 threads fit on an SM, so the 1040 CTAs of a
-// 65 x 512-line grid run in one wave on 152 SMs with the most loads in flight per thread (334 us at
+// 65 x 512-line grid run in one wave on 152 SMs with the most loads in flight per thread (332 us at
 // 65x512x512; 80 registers: 6 CTAs per SM and a second wave, 530 us; the compiler's own choice of 48
-// registers: 415 us).  A bound of 6 blocks gives the whole-grid instance 72 registers and its fastest code
-// (a bound of 7 also gives 72 registers but scheduled differently: 347-363 us); check -Xptxas -v after a
-// change.
+// registers: 415 us; a bound of 7 blocks also gives 72 registers but schedules worse: 347-363 us).  The
+// whole-grid kernels set the budget directly (__maxnreg__); the host-buffer step's line-range kernels keep a
+// bound of 6 blocks (kXMinBlocks).  Check -Xptxas -v after a change.
 constexpr int kXMinBlocks = 6;
 constexpr int kLineThreads = 128;
 
@@ -54,25 +54,11 @@ __device__ __forceinline__ uint64_t l2_policy_last() {
 __device__ __forceinline__ void st_keep(double* p, double v, uint64_t policy) {
   asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(v), "l"(policy) : "memory");
 }
-__device__ __forceinline__ uint64_t l2_policy_first() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-// a read-only load carrying an L2 policy (evict-first: streamed data that should not displace the round trip)
-template <bool HINT>
-__device__ __forceinline__ double ldc(const double* p, uint64_t policy) {
-  if (!HINT) return *p;
-  double v;
-  asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(policy));
-  return v;
-}
-
-template <bool HAS_Q, bool HINT = false>
+template <bool HAS_Q>
 __device__ __forceinline__ double stencil_x(const Dims& d, const double* __restrict__ T, const Coeffs& c,
                                             const uint8_t* __restrict__ vclass, const double* __restrict__ qdense,
                                             const double* __restrict__ qshape, const double* sq, int64_t L, int ch,
-                                            int lane, uint64_t first = 0) {
+                                            int lane) {
   const int64_t i = (int64_t)ch * 32 + lane;
   const int64_t k = L / d.ny, j = L - k * d.ny;
   const int64_t p = L * d.nx + i;
@@ -85,13 +71,13 @@ __device__ __forceinline__ double stencil_x(const Dims& d, const double* __restr
   const double tyh = j + 1 < d.ny ? T[p + d.nx] : t;
   const double tzl = k > 0 ? T[p - nxy] : t;
   const double tzh = k + 1 < d.nz ? T[p + nxy] : t;
-  double r = ldc<HINT>(w + kWc * 32, first) * t;
-  r = fma(ldc<HINT>(w + kWxl * 32, first), txl, r);
-  r = fma(ldc<HINT>(w + kWxh * 32, first), txh, r);
-  r = fma(ldc<HINT>(w + kWyl * 32, first), tyl, r);
-  r = fma(ldc<HINT>(w + kWyh * 32, first), tyh, r);
-  r = fma(ldc<HINT>(w + kWzl * 32, first), tzl, r);
-  r = fma(ldc<HINT>(w + kWzh * 32, first), tzh, r);
+  double r = w[kWc * 32] * t;
+  r = fma(w[kWxl * 32], txl, r);
+  r = fma(w[kWxh * 32], txh, r);
+  r = fma(w[kWyl * 32], tyl, r);
+  r = fma(w[kWyh * 32], tyh, r);
+  r = fma(w[kWzl * 32], tzl, r);
+  r = fma(w[kWzh * 32], tzh, r);
   if (HAS_Q) {
     double q = sq[vclass[p]];
     if (qshape) q *= qshape[p];
@@ -115,7 +101,7 @@ __device__ __forceinline__ int64_t w0_index(const Dims& d, const Coeffs& c, int6
   return L * c.px + i;
 }
 
-template <bool HAS_Q, bool RANGED, int LINES, int PITCHED, bool HINT = false>
+template <bool HAS_Q, bool RANGED, int LINES, int PITCHED>
 __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __restrict__ T, const Coeffs& c,
                                              const uint8_t* __restrict__ vclass, const double* __restrict__ qdense,
                                              const double* __restrict__ qshape, const QTable& qt,
@@ -131,7 +117,6 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
   const int64_t nlines = RANGED ? line_end : d.nz * d.ny;
   const int64_t L0 = (RANGED ? line_begin : 0) + (int64_t)blockIdx.x * LINES;
   const int nchunks = (int)((d.nx + kXChunk - 1) / kXChunk);
-  const uint64_t first = HINT ? l2_policy_first() : 0, keep = HINT ? l2_policy_last() : 0;
   __syncthreads();
 
   // forward: z_i = R'_i - a0_i * z_{i-1}
@@ -144,8 +129,8 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
       const int64_t L = L0 + l;
       double r = 0.0, a = 0.0;
       if (L < nlines && i < d.nx) {
-        r = stencil_x<HAS_Q, HINT>(d, T, c, vclass, qdense, qshape, sq, L, ch, lane, first);
-        a = ldc<HINT>(c.a0 + L * d.nx + i, first);
+        r = stencil_x<HAS_Q>(d, T, c, vclass, qdense, qshape, sq, L, ch, lane);
+        a = c.a0[L * d.nx + i];
       }
       sr[l][lane] = r;
       sa[l][lane] = a;
@@ -166,12 +151,7 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
     for (int ll = 0; ll < kPerWarp; ++ll) {
       const int l = warp * kPerWarp + ll;
       const int64_t L = L0 + l;
-      if (L < nlines && i < d.nx) {
-        if (HINT)
-          st_keep(W0 + w0_index<PITCHED>(d, c, L, i), sr[l][lane], keep);
-        else
-          W0[w0_index<PITCHED>(d, c, L, i)] = sr[l][lane];
-      }
+      if (L < nlines && i < d.nx) W0[w0_index<PITCHED>(d, c, L, i)] = sr[l][lane];
     }
     __syncthreads();
   }
@@ -188,7 +168,7 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
       if (L < nlines && i < d.nx) {
         const int64_t p = L * d.nx + i;
         z = W0[w0_index<PITCHED>(d, c, L, i)];
-        b = ldc<HINT>(c.b0 + p, first);
+        b = c.b0[p];
       }
       sr[l][lane] = z;
       sa[l][lane] = b;
@@ -215,8 +195,21 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
   }
 }
 
-// The x sweep of almost every step (no source term, W0 rows unpadded): 72 registers under a bound of 6 blocks,
-// its fastest schedule (334 us at 65x512x512).  Also the line-range instances of the host-buffer step.
+// The x sweep over the whole grid: the register budget is set to 72, which keeps 7 CTAs of 128 threads per SM, so
+// the 1040 CTAs of a 65x512-line grid run in one wave (332 us at 65x512x512; under a bound of 6 blocks the
+// instance without a source also gets 72 registers and takes 334 us, while the instances with a source term or
+// padded W0 rows take 78-80 registers there, 6 CTAs per SM, two waves: 694 us for a source step).  Padded rows
+// of an odd nx use the one-column index (349 us at 65x512x511; with a general pitch 362 us).
+template <bool HAS_Q, bool RANGED, int LINES, int PITCH>
+__global__ void __maxnreg__(72) sweep_x_lean_kernel(Dims d, const double* __restrict__ T, Coeffs c,
+                                                    const uint8_t* __restrict__ vclass,
+                                                    const double* __restrict__ qdense,
+                                                    const double* __restrict__ qshape, QTable qt,
+                                                    double* __restrict__ W0, int64_t line_begin, int64_t line_end) {
+  sweep_x_body<HAS_Q, RANGED, LINES, PITCH>(d, T, c, vclass, qdense, qshape, qt, W0, line_begin, line_end);
+}
+// The line ranges of the host-buffer step on unpadded rows keep the 6-block bound (80 registers at 32 lines per
+// CTA): measured against the 72-register build there, 9.62e9 against 9.39e9 voxel-steps/s end to end.
 template <bool HAS_Q, bool RANGED, int LINES = kXLines>
 __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d, const double* __restrict__ T, Coeffs c,
                                                              const uint8_t* __restrict__ vclass,
@@ -225,18 +218,6 @@ __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d,
                                                              double* __restrict__ W0, int64_t line_begin,
                                                              int64_t line_end) {
   sweep_x_body<HAS_Q, RANGED, LINES, 0>(d, T, c, vclass, qdense, qshape, qt, W0, line_begin, line_end);
-}
-// The whole-grid sweep with a source term or with padded W0 rows: under the 6-block bound these take 78-80
-// registers, 6 CTAs per SM, so the 1040 CTAs of a 65x512-line grid run in two waves (694 us for a source step);
-// their register budget is set directly to the 72 that keep 7 CTAs per SM (padded rows of an odd nx with the
-// one-column index: 349 us at 65x512x511; with a general pitch: 362 us).
-template <bool HAS_Q, bool RANGED, int LINES, int PITCH, bool HINT = false>
-__global__ void __maxnreg__(72) sweep_x_lean_kernel(Dims d, const double* __restrict__ T, Coeffs c,
-                                                    const uint8_t* __restrict__ vclass,
-                                                    const double* __restrict__ qdense,
-                                                    const double* __restrict__ qshape, QTable qt,
-                                                    double* __restrict__ W0, int64_t line_begin, int64_t line_end) {
-  sweep_x_body<HAS_Q, RANGED, LINES, PITCH, HINT>(d, T, c, vclass, qdense, qshape, qt, W0, line_begin, line_end);
 }
 
 // x sweep over all lines (RANGED false) or the lines [line_begin, line_end) of the host-buffer step
@@ -250,12 +231,7 @@ void launch_x(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_
 #define HS2G_X(KERNEL, ...) \
   KERNEL<__VA_ARGS__><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, a.qshape, q, a.W0, line_begin, \
                                                line_end)
-  const char* xv = getenv("HS2G_X_VARIANT");
-  if (!RANGED && pitch == 0 && !has_q && xv && strcmp(xv, "lean") == 0) {
-    HS2G_X(sweep_x_lean_kernel, false, false, LINES, 0, false);
-  } else if (!RANGED && pitch == 0 && !has_q && xv && strcmp(xv, "lean_hint") == 0) {
-    HS2G_X(sweep_x_lean_kernel, false, false, LINES, 0, true);
-  } else if (pitch == 0 && (!has_q || RANGED)) {
+  if (RANGED && pitch == 0) {
     if (has_q)
       HS2G_X(sweep_x_kernel, true, RANGED, LINES);
     else
