@@ -17,7 +17,7 @@ OK = 0
 ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_EXTERIOR, ERR_KTYPE, ERR_UNALIGNED, ERR_FORM, ERR_CAPACITY, ERR_STATE = \
     -1, -2, -3, -4, -5, -6, -7, -8, -9
 ERR_TIMEOUT = -10
-DEVICE, SYNC, REUSE = 1, 2, 4
+DEVICE, SYNC, REUSE, SCHEDULED = 1, 2, 4, 8
 SHAPED_IMPULSE = 5
 K_ENTRIES = 10
 FORM_LEN = 1 + 2 * K_ENTRIES
@@ -34,7 +34,7 @@ EXPORTED = ("hs2g_abi_version", "hs2g_last_error", "hs2g_create_classes", "hs2g_
             "hs2g_adjoint_device_bytes", "hs2g_adjoint_set_parameters", "hs2g_adjoint_forward",
             "hs2g_adjoint_backward", "hs2g_create_rows", "hs2g_selftest_wait", "hs2g_run_surface",
             "hs2g_surface_temperature", "hs2g_set_source_classes", "hs2g_source_zdecay", "hs2g_source_point",
-            "hs2g_adjoint_set_faces")
+            "hs2g_adjoint_set_faces", "hs2g_set_schedule", "hs2g_set_clock", "hs2g_get_clock")
 STATIC_MAX_VOXELS = 1 << 20
 
 
@@ -134,6 +134,12 @@ def load():
         L.hs2g_source_table.restype = i32
         L.hs2g_set_source_classes.argtypes = [vp, vp, i32]
         L.hs2g_set_source_classes.restype = i32
+        L.hs2g_set_schedule.argtypes = [vp, ctypes.c_int64, vp, i32]
+        L.hs2g_set_schedule.restype = i32
+        L.hs2g_set_clock.argtypes = [vp, ctypes.c_int64]
+        L.hs2g_set_clock.restype = i32
+        L.hs2g_get_clock.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+        L.hs2g_get_clock.restype = i32
         L.hs2g_source_zdecay.argtypes = [vp, i32, vp, dp, dp, dp, dp, dp, dp, i32]
         L.hs2g_source_zdecay.restype = i32
         L.hs2g_source_point.argtypes = [vp, i32, vp, i64, vp, dp, dp, i32]

@@ -1,6 +1,7 @@
 // C ABI of the hs2g library (declared in include/hs2g.h).  Host-side runtime: owns device buffers, compiles a
 // problem into step coefficients and queues timesteps on a stream.
 #include <cmath>
+#include <cstddef>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -71,6 +72,23 @@ struct hs2g_handle {
   cudaStream_t copy_stream = nullptr;
   cudaStream_t x_stream[kCopyChunks] = {};
   cudaEvent_t ev_in[kCopyChunks] = {}, ev_x[kCopyChunks] = {}, ev_out[kCopyChunks] = {}, ev_begin = nullptr;
+  // device source schedule (hs2g_set_schedule): the descriptor the scheduled x sweep reads, its rows and flags
+  hs2g::DevSchedule* sched_dev = nullptr;
+  double* sched_q = nullptr;
+  uint8_t* sched_active = nullptr;
+  int64_t sched_cap = 0, sched_n = 0;
+  // captured in-place step graphs of hs2g_run, keyed by what they bake in; captured on a stream of their own
+  // (capture is not allowed on the legacy default stream the caller may have chosen) and launched on `stream`
+  struct StepGraph {
+    double* T;
+    double* hist;
+    int layer;
+    double dz2;
+    bool scheduled;
+    cudaGraphExec_t exec;
+  };
+  std::vector<StepGraph> graphs;
+  cudaStream_t cap_stream = nullptr;
 };
 
 namespace {
@@ -441,7 +459,7 @@ void hs2g_destroy(hs2g_handle* h) {
   dfree(h, h->Tin_dev, n);
   dfree(h, h->Tout_dev, n);
   dfree(h, h->qdense_dev, n);
-  dfree(h, h->hist_dev, 0);
+  dfree(h, h->hist_dev, h->hist_len);
   dfree(h, h->qshape, n);
   for (int c = 0; c < HS2G_MAX_CLASSES; ++c) {
     dfree(h, h->shape_zgrid[c], n);
@@ -461,6 +479,11 @@ void hs2g_destroy(hs2g_handle* h) {
     if (h->ev_out[c]) cudaEventDestroy(h->ev_out[c]);
   }
   if (h->ev_begin) cudaEventDestroy(h->ev_begin);
+  for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
+  if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+  dfree(h, h->sched_dev, 1);
+  dfree(h, h->sched_q, h->sched_cap * HS2G_MAX_CLASSES);
+  dfree(h, h->sched_active, h->sched_cap);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
 }
@@ -787,8 +810,108 @@ int hs2g_step(hs2g_handle* h, const double* T_in, double* T_out, const double* q
 }
 
 namespace {
+int ensure_schedule(hs2g_handle* h) {
+  if (h->sched_dev) return HS2G_OK;
+  int rc = dalloc(h, &h->sched_dev, 1, "source schedule");
+  if (rc) return rc;
+  HS2G_CUDA(cudaMemsetAsync(h->sched_dev, 0, sizeof(hs2g::DevSchedule), h->stream), "clear source schedule");
+  return HS2G_OK;
+}
+
+// Queue the host-owned fields of the schedule descriptor (rows, flags, row count, shape field) on the handle's
+// stream; the clock fields are left as they are.  The descriptor names the shape field only while some class has
+// a shape: a voxel's class value is multiplied by its shape value, which is 1 for every voxel of a class without
+// one, so the product is exact for those classes.
+int write_schedule_header(hs2g_handle* h) {
+  bool any_shape = false;
+  for (int c = 0; c < HS2G_MAX_CLASSES && h->qshape; ++c) any_shape |= h->shaped[c];
+  const hs2g::DevSchedule hdr{h->sched_q, h->sched_active, any_shape ? h->qshape : nullptr, h->sched_n, 0, 0};
+  // a pageable source is staged before the call returns, so the local descriptor may go out of scope
+  HS2G_CUDA(cudaMemcpyAsync(h->sched_dev, &hdr, offsetof(hs2g::DevSchedule, step), cudaMemcpyHostToDevice,
+                            h->stream),
+            "write source schedule");
+  return HS2G_OK;
+}
+
+int set_clock(hs2g_handle* h, int64_t step) {
+  HS2G_CUDA(cudaMemcpyAsync(&h->sched_dev->step, &step, sizeof(step), cudaMemcpyHostToDevice, h->stream),
+            "set schedule clock");
+  return HS2G_OK;
+}
+
+// Replace the schedule's rows by qtabs[nsteps][HS2G_MAX_CLASSES] (host, or device when device_ptr) and set the
+// clock to 0.  Work already queued on the handle's stream reads the old rows before they are overwritten.
+int set_schedule_rows(hs2g_handle* h, int64_t nsteps, const double* qtabs, bool device_ptr) {
+  int rc = ensure_schedule(h);
+  if (rc) return rc;
+  if (nsteps > h->sched_cap) {
+    HS2G_CUDA(cudaStreamSynchronize(h->stream), "source schedule");  // queued steps may read the old rows
+    dfree(h, h->sched_q, h->sched_cap * HS2G_MAX_CLASSES);
+    dfree(h, h->sched_active, h->sched_cap);
+    h->sched_cap = h->sched_n = 0;
+    if ((rc = dalloc(h, &h->sched_q, nsteps * HS2G_MAX_CLASSES, "source schedule rows"))) return rc;
+    if ((rc = dalloc(h, &h->sched_active, nsteps, "source schedule flags"))) return rc;
+    h->sched_cap = nsteps;
+  }
+  if (nsteps > 0) {
+    HS2G_CUDA(cudaMemcpyAsync(h->sched_q, qtabs, sizeof(double) * HS2G_MAX_CLASSES * (size_t)nsteps,
+                              device_ptr ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream),
+              "upload source schedule");
+    HS2G_CUDA(hs2g::launch_schedule_flags(h->sched_q, nsteps, h->sched_active, h->stream), "schedule flags");
+  }
+  h->sched_n = nsteps;
+  if ((rc = write_schedule_header(h))) return rc;
+  return set_clock(h, 0);
+}
+
+// One step src -> dst whose sources come from the schedule at its clock (or none), with the history row and the
+// clock tick after it, queued on stream s.
+cudaError_t queue_step(hs2g_handle* h, const double* src, double* dst, double* hist, int layer, double dz2,
+                       bool scheduled, cudaStream_t s) {
+  hs2g::StepArgs a = make_args(h, src, dst);
+  a.T_in = src;
+  a.T_out = dst;
+  cudaError_t e = hs2g::launch_step_scheduled(a, h->c, scheduled ? h->sched_dev : nullptr, s);
+  if (e == cudaSuccess && hist) e = hs2g::launch_history_row(h->d, dst, layer, dz2, hist, h->sched_dev, s);
+  if (e == cudaSuccess && (scheduled || hist)) e = hs2g::launch_tick(h->sched_dev, scheduled ? 1 : 0, s);
+  return e;
+}
+
+// The captured in-place step on T (T_in == T_out == T), from the handle's cache or captured now.
+constexpr size_t kMaxStepGraphs = 8;
+int step_graph(hs2g_handle* h, double* T, double* hist, int layer, double dz2, bool scheduled,
+               cudaGraphExec_t* out) {
+  for (const auto& g : h->graphs)
+    if (g.T == T && g.hist == hist && g.layer == layer && g.dz2 == dz2 && g.scheduled == scheduled) {
+      *out = g.exec;
+      return HS2G_OK;
+    }
+  if (!h->cap_stream)
+    HS2G_CUDA(cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking), "capture stream");
+  HS2G_CUDA(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal), "begin step capture");
+  cudaError_t e = queue_step(h, T, T, hist, layer, dz2, scheduled, h->cap_stream);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e_end = cudaStreamEndCapture(h->cap_stream, &g);
+  if (e == cudaSuccess) e = e_end;
+  cudaGraphExec_t exec = nullptr;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return cuda_fail(e, "capture of the step graph");
+  }
+  if (h->graphs.size() >= kMaxStepGraphs) {  // a graph still executing is released when it completes
+    cudaGraphExecDestroy(h->graphs.front().exec);
+    h->graphs.erase(h->graphs.begin());
+  }
+  h->graphs.push_back({T, hist, layer, dz2, scheduled, exec});
+  *out = exec;
+  return HS2G_OK;
+}
+
 // hs2g_run and hs2g_run_surface: after every step, history receives layer record_layer of T, or (surface_dz > 0)
-// the insulating z = 0 surface temperature estimated from layers 0 and 1
+// the insulating z = 0 surface temperature estimated from layers 0 and 1.  The first step of a call with
+// T_in != T_out is queued directly; every further step is one replay of the captured in-place step graph.
 int run_steps(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, const double* qtabs, int record_layer,
               double surface_dz, double* history, int flags) {
   DeviceGuard g(h->device);
@@ -797,11 +920,19 @@ int run_steps(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, con
   const int64_t n = d.nvox();
   const bool dev = (flags & HS2G_DEVICE) != 0;
   cudaStream_t s = h->stream;
+  int rc = ensure_schedule(h);
+  if (rc) return rc;
+  bool scheduled = (flags & HS2G_SCHEDULED) != 0;
+  if (qtabs) {
+    if ((rc = set_schedule_rows(h, nsteps, qtabs, false))) return rc;
+    scheduled = true;
+  } else if ((rc = write_schedule_header(h))) {  // the shape field may have changed since the schedule was set
+    return rc;
+  }
   const double* src = T_in;
   double* dst = T_out;
   if (!dev) {
-    int rc = ensure_staging(h);
-    if (rc) return rc;
+    if ((rc = ensure_staging(h))) return rc;
     HS2G_CUDA(cudaMemcpyAsync(h->Tin_dev, T_in, sizeof(double) * n, cudaMemcpyHostToDevice, s), "upload T");
     src = h->Tin_dev;
     dst = h->Tout_dev;
@@ -814,38 +945,26 @@ int run_steps(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, con
       const int64_t need = (int64_t)nsteps * d.nxy();
       if (need > h->hist_len) {
         dfree(h, h->hist_dev, h->hist_len);
-        int rc = dalloc(h, &h->hist_dev, need, "surface history");
-        if (rc) return rc;
+        h->hist_len = 0;
+        if ((rc = dalloc(h, &h->hist_dev, need, "surface history"))) return rc;
         h->hist_len = need;
       }
       hist = h->hist_dev;
     }
+    HS2G_CUDA(cudaMemsetAsync(&h->sched_dev->row, 0, sizeof(int64_t), s), "reset history row");
   }
-  hs2g::StepArgs a = make_args(h, src, dst);
-  hs2g::QTable q;
-  memset(&q, 0, sizeof(q));
-  for (int st = 0; st < nsteps; ++st) {
-    a.has_qtab = false;
-    a.qshape = nullptr;
-    if (qtabs) {
-      const double* qt = qtabs + (int64_t)st * HS2G_MAX_CLASSES;
-      for (int c = 0; c < HS2G_MAX_CLASSES; ++c) {
-        q.q[c] = qt[c];
-        if (qt[c] != 0.0) a.has_qtab = true;
-      }
-      a.qshape = active_shape(h, qt);
-    }
-    a.T_in = src;
-    a.T_out = dst;
-    cudaError_t e = hs2g::launch_step(a, h->c, q, s);
+  const int layer = hist && surface_dz <= 0.0 ? record_layer : 0;
+  const double dz2 = hist && surface_dz > 0.0 ? hs2g::surface_dz2(surface_dz) : 0.0;
+  int done = 0;
+  if (nsteps > 0 && src != dst) {
+    cudaError_t e = queue_step(h, src, dst, hist, layer, dz2, scheduled, s);
     if (e != cudaSuccess) return cuda_fail(e, "step kernels");
-    if (hist) {
-      double* row = hist + (int64_t)st * d.nxy();
-      e = surface_dz > 0.0 ? hs2g::launch_surface_estimate(d.nxy(), dst, surface_dz, row, s)
-                           : hs2g::launch_copy_layer(d, dst, record_layer, row, s);
-      if (e != cudaSuccess) return cuda_fail(e, "history copy");
-    }
-    src = dst;
+    done = 1;
+  }
+  if (done < nsteps) {
+    cudaGraphExec_t graph = nullptr;
+    if ((rc = step_graph(h, dst, hist, layer, dz2, scheduled, &graph))) return rc;
+    for (; done < nsteps; ++done) HS2G_CUDA(cudaGraphLaunch(graph, s), "step graph");
   }
   if (nsteps == 0 && src != dst) {
     HS2G_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, s), "copy T");
@@ -864,6 +983,36 @@ int run_steps(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, con
   return HS2G_OK;
 }
 }  // namespace
+
+int hs2g_set_schedule(hs2g_handle* h, int64_t nsteps, const double* qtabs, int flags) {
+  if (!h || nsteps < 0 || (nsteps > 0 && !qtabs)) return fail(HS2G_ERR_ARG, "hs2g_set_schedule: bad argument");
+  DeviceGuard g(h->device);
+  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", h->device);
+  int rc = set_schedule_rows(h, nsteps, qtabs, (flags & HS2G_DEVICE) != 0);
+  if (rc) return rc;
+  if (flags & HS2G_SYNC) HS2G_CUDA(cudaStreamSynchronize(h->stream), "hs2g_set_schedule");
+  return HS2G_OK;
+}
+
+int hs2g_set_clock(hs2g_handle* h, int64_t step) {
+  if (!h || step < 0) return fail(HS2G_ERR_ARG, "hs2g_set_clock: bad argument");
+  DeviceGuard g(h->device);
+  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", h->device);
+  int rc = ensure_schedule(h);
+  return rc ? rc : set_clock(h, step);
+}
+
+int hs2g_get_clock(hs2g_handle* h, int64_t* step) {
+  if (!h || !step) return fail(HS2G_ERR_ARG, "hs2g_get_clock: bad argument");
+  DeviceGuard g(h->device);
+  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", h->device);
+  int rc = ensure_schedule(h);
+  if (rc) return rc;
+  HS2G_CUDA(cudaMemcpyAsync(step, &h->sched_dev->step, sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream),
+            "read schedule clock");
+  HS2G_CUDA(cudaStreamSynchronize(h->stream), "read schedule clock");
+  return HS2G_OK;
+}
 
 int hs2g_run(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, const double* qtabs,
              int record_layer, double* history, int flags) {

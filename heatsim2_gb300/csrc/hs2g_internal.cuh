@@ -44,6 +44,19 @@ struct QTable {
   double q[HS2G_MAX_CLASSES];
 };
 
+// Device-resident source schedule of a handle, read by the scheduled x sweep at the start of every step.  The
+// first four fields are written by the host when the schedule or the source shapes change; `step` (the
+// schedule row of the next step) and `row` (the history row of the next step of the current run) are advanced
+// on the device by the step's last kernel, so that one captured step graph replays any number of steps.
+struct DevSchedule {
+  const double* q;         // [n][HS2G_MAX_CLASSES] class source values (W/m^3)
+  const uint8_t* active;   // [n] 1 when row s has a non-zero value
+  const double* shape;     // per-voxel multiplier of the class sources, or null when no class has a shape
+  int64_t n;               // rows; steps at or beyond n have no source
+  int64_t step;
+  int64_t row;
+};
+
 // Record the message hs2g_last_error() returns for this thread (hs2g_api.cu); returns code.
 int set_last_error(int code, const char* message);
 
@@ -111,6 +124,19 @@ cudaError_t launch_step(const StepArgs& a, const Coeffs& c, const QTable& q, cud
 // the same three kernels with an event recorded before each and after the last (ev[0..3])
 cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s,
                                cudaEvent_t ev[4]);
+// One step whose class sources come from the device schedule ds at its clock (ds null: no source); the x sweep
+// decides on the device whether the step has a source.  Used for the captured step graph of hs2g_run.
+cudaError_t launch_step_scheduled(const StepArgs& a, const Coeffs& c, const DevSchedule* ds, cudaStream_t s);
+// History of the step just taken into hist[ds->row][ny][nx]: layer `layer` of T (dz2 <= 0) or the insulating
+// z = 0 surface estimate from layers 0 and 1 with dz2 = dz**2 (dz2 > 0).
+cudaError_t launch_history_row(const Dims& d, const double* T, int layer, double dz2, double* hist,
+                               const DevSchedule* ds, cudaStream_t s);
+// Advance the schedule clock after a step: row += 1, and step += 1 when advance_step.
+cudaError_t launch_tick(DevSchedule* ds, int advance_step, cudaStream_t s);
+// the reference's dz**2.0 (the C library's pow)
+double surface_dz2(double dz);
+// one flag per schedule row: active[s] = any of q[s][0..nclass-1] non-zero
+cudaError_t launch_schedule_flags(const double* q, int64_t nrows, uint8_t* active, cudaStream_t s);
 cudaError_t fp64_fma_rate(double* fma_per_s);
 cudaError_t launch_copy_layer(const Dims& d, const double* T, int layer, double* dst, cudaStream_t s);
 // insulating z = 0 surface temperature from layers 0 and 1 of T (an nxy-element plane each) into dst[nxy]

@@ -101,18 +101,24 @@ __device__ __forceinline__ int64_t w0_index(const Dims& d, const Coeffs& c, int6
   return L * c.px + i;
 }
 
-template <bool HAS_Q, bool RANGED, int LINES, int PITCHED>
+// The class source values come from the kernel's parameter table qt, or (QROW) from the global row qrow.  The
+// kernel owns the shared arrays: sr, sa [LINES][kXChunk + 1] and sq [HS2G_MAX_CLASSES when HAS_Q].
+template <bool HAS_Q, bool RANGED, int LINES, int PITCHED, bool QROW = false, typename QT = QTable>
 __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __restrict__ T, const Coeffs& c,
                                              const uint8_t* __restrict__ vclass, const double* __restrict__ qdense,
-                                             const double* __restrict__ qshape, const QTable& qt,
-                                             double* __restrict__ W0, int64_t line_begin, int64_t line_end) {
+                                             const double* __restrict__ qshape, const QT& qt,
+                                             const double* __restrict__ qrow, double* __restrict__ W0,
+                                             int64_t line_begin, int64_t line_end, double (*sr)[kXChunk + 1],
+                                             double (*sa)[kXChunk + 1], double* sq) {
   constexpr int kPerWarp = LINES / kXWarps;
-  __shared__ double sr[LINES][kXChunk + 1];
-  __shared__ double sa[LINES][kXChunk + 1];
-  __shared__ double sq[HAS_Q ? HS2G_MAX_CLASSES : 1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (HAS_Q) {
-    for (int e = threadIdx.x; e < HS2G_MAX_CLASSES; e += kXThreads) sq[e] = qt.q[e];
+  if constexpr (HAS_Q) {
+    for (int e = threadIdx.x; e < HS2G_MAX_CLASSES; e += kXThreads) {
+      if constexpr (QROW)
+        sq[e] = qrow[e];
+      else
+        sq[e] = qt.q[e];
+    }
   }
   const int64_t nlines = RANGED ? line_end : d.nz * d.ny;
   const int64_t L0 = (RANGED ? line_begin : 0) + (int64_t)blockIdx.x * LINES;
@@ -206,7 +212,11 @@ __global__ void __maxnreg__(72) sweep_x_lean_kernel(Dims d, const double* __rest
                                                     const double* __restrict__ qdense,
                                                     const double* __restrict__ qshape, QTable qt,
                                                     double* __restrict__ W0, int64_t line_begin, int64_t line_end) {
-  sweep_x_body<HAS_Q, RANGED, LINES, PITCH>(d, T, c, vclass, qdense, qshape, qt, W0, line_begin, line_end);
+  __shared__ double sr[LINES][kXChunk + 1];
+  __shared__ double sa[LINES][kXChunk + 1];
+  __shared__ double sq[HAS_Q ? HS2G_MAX_CLASSES : 1];
+  sweep_x_body<HAS_Q, RANGED, LINES, PITCH>(d, T, c, vclass, qdense, qshape, qt, nullptr, W0, line_begin, line_end,
+                                            sr, sa, sq);
 }
 // The line ranges of the host-buffer step on unpadded rows keep the 6-block bound (80 registers at 32 lines per
 // CTA): measured against the 72-register build there, 9.62e9 against 9.39e9 voxel-steps/s end to end.
@@ -217,7 +227,39 @@ __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d,
                                                              const double* __restrict__ qshape, QTable qt,
                                                              double* __restrict__ W0, int64_t line_begin,
                                                              int64_t line_end) {
-  sweep_x_body<HAS_Q, RANGED, LINES, 0>(d, T, c, vclass, qdense, qshape, qt, W0, line_begin, line_end);
+  __shared__ double sr[LINES][kXChunk + 1];
+  __shared__ double sa[LINES][kXChunk + 1];
+  __shared__ double sq[HAS_Q ? HS2G_MAX_CLASSES : 1];
+  sweep_x_body<HAS_Q, RANGED, LINES, 0>(d, T, c, vclass, qdense, qshape, qt, nullptr, W0, line_begin, line_end, sr,
+                                        sa, sq);
+}
+
+// The x sweep of a scheduled step (the captured step graph of hs2g_run): the class table is row ds->step of the
+// handle's device schedule, read here, and the CTA takes the source body or the plain one by the row's flag, so
+// one launch serves the steps with and without a source.  Both bodies share the kernel's shared arrays.
+template <int PITCH>
+__global__ void __maxnreg__(72) sweep_x_sched_kernel(Dims d, const double* __restrict__ T, Coeffs c,
+                                                     const uint8_t* __restrict__ vclass,
+                                                     const DevSchedule* __restrict__ ds, double* __restrict__ W0) {
+  __shared__ double sr[kXLines][kXChunk + 1];
+  __shared__ double sa[kXLines][kXChunk + 1];
+  __shared__ double sq[HS2G_MAX_CLASSES];
+  const double* qrow = nullptr;
+  const double* shape = nullptr;
+  if (ds) {
+    const int64_t st = ds->step;
+    if (st >= 0 && st < ds->n && ds->active[st]) {
+      qrow = ds->q + st * HS2G_MAX_CLASSES;
+      shape = ds->shape;
+    }
+  }
+  const int no_table = 0;  // the table comes from qrow
+  if (qrow)
+    sweep_x_body<true, false, kXLines, PITCH, true>(d, T, c, vclass, nullptr, shape, no_table, qrow, W0, 0, 0, sr,
+                                                    sa, sq);
+  else
+    sweep_x_body<false, false, kXLines, PITCH, true>(d, T, c, vclass, nullptr, nullptr, no_table, nullptr, W0, 0, 0,
+                                                     sr, sa, sq);
 }
 
 // x sweep over all lines (RANGED false) or the lines [line_begin, line_end) of the host-buffer step
@@ -253,6 +295,18 @@ void launch_x(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_
       HS2G_X(sweep_x_lean_kernel, false, RANGED, LINES, 2);
   }
 #undef HS2G_X
+}
+
+void launch_x_sched(const StepArgs& a, const Coeffs& c, const DevSchedule* ds, cudaStream_t s) {
+  const Dims& d = a.d;
+  const unsigned gx = (unsigned)((d.nz * d.ny + kXLines - 1) / kXLines);
+  const int pitch = c.px == d.nx ? 0 : c.px == d.nx + 1 ? 1 : 2;
+  if (pitch == 0)
+    sweep_x_sched_kernel<0><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, a.W0);
+  else if (pitch == 1)
+    sweep_x_sched_kernel<1><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, a.W0);
+  else
+    sweep_x_sched_kernel<2><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, a.W0);
 }
 
 // y lines: W1 = s2 * dT1 from W0 = sigma * dT0
@@ -319,18 +373,44 @@ __global__ void copy_layer_kernel(Dims d, const double* __restrict__ T, int laye
 // insulating_z_min_surface_temperature(T, dz) does (surface_temperature.py:4-36): the mean of a quadratic with
 // zero slope at the surface through the two layer centres, c = T0 - (0.25 a) dz^2 with a = (T1 - T0)/(2 dz^2),
 // and the linear extrapolation T0 - (T1 - T0)/2.  Same operations in the same order, each rounding explicit.
-__global__ void surface_estimate_kernel(int64_t nxy, const double* __restrict__ T, double dz2,
-                                        double* __restrict__ dst) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= nxy) return;
-  const double t0 = T[t], t1 = T[nxy + t];
+__device__ __forceinline__ double surface_value(double t0, double t1, double dz2) {
   const double a = __ddiv_rn(__dsub_rn(t1, t0), __dmul_rn(2.0, dz2));
   const double c = __dsub_rn(t0, __dmul_rn(__dmul_rn(0.25, a), dz2));
   const double lin = __dsub_rn(t0, __ddiv_rn(__dsub_rn(t1, t0), 2.0));
-  dst[t] = __ddiv_rn(__dadd_rn(lin, c), 2.0);
+  return __ddiv_rn(__dadd_rn(lin, c), 2.0);
+}
+__global__ void surface_estimate_kernel(int64_t nxy, const double* __restrict__ T, double dz2,
+                                        double* __restrict__ dst) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t < nxy) dst[t] = surface_value(T[t], T[nxy + t], dz2);
 }
 
 inline unsigned blocks(int64_t n, int per) { return (unsigned)((n + per - 1) / per); }
+// History of a scheduled step into row ds->row of hist: layer `layer` of T, or (dz2 > 0) the surface estimate.
+__global__ void history_row_kernel(int64_t nxy, const double* __restrict__ T, int layer, double dz2,
+                                   double* __restrict__ hist, const DevSchedule* __restrict__ ds) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nxy) return;
+  double* dst = hist + ds->row * nxy;
+  dst[t] = dz2 > 0.0 ? surface_value(T[t], T[nxy + t], dz2) : T[(int64_t)layer * nxy + t];
+}
+
+// The last node of a scheduled step: every kernel of the step that reads the clock has completed.
+__global__ void tick_kernel(DevSchedule* ds, int advance_step) {
+  ds->row += 1;
+  if (advance_step) ds->step += 1;
+}
+
+__global__ void schedule_flags_kernel(const double* __restrict__ q, int64_t nrows, uint8_t* __restrict__ active) {
+  const int64_t r = blockIdx.x * (int64_t)(blockDim.x / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= nrows) return;
+  bool any = false;
+  for (int c = lane; c < HS2G_MAX_CLASSES; c += 32) any |= q[r * HS2G_MAX_CLASSES + c] != 0.0;
+  any = __any_sync(0xffffffffu, any);
+  if (lane == 0) active[r] = any ? 1 : 0;
+}
+
 
 // FP64 issue-rate probe: 8 independent FMA chains per thread, registers only, one store per thread.
 __global__ void fp64_probe_kernel(double* out, int iters, double a, double b) {
@@ -379,12 +459,10 @@ cudaError_t fp64_fma_rate(double* fma_per_s) {
   return e;
 }
 
-cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s,
-                               cudaEvent_t ev[4]) {
+namespace {
+// the y and z sweeps of a step, with events before each and after the last when ev is given
+cudaError_t launch_yz(const StepArgs& a, const Coeffs& c, cudaStream_t s, cudaEvent_t* ev) {
   const Dims& d = a.d;
-  if (ev) cudaEventRecord(ev[0], s);
-  launch_x<false, kXLines>(a, c, q, 0, 0, s);
-  if (ev) cudaEventRecord(ev[1], s);
   cudaError_t e = cudaSuccess;
   if (a.bulk_y)
     e = launch_lines_bulk(d, 1, a.W0, c.a1, a.W1, c.b1, nullptr, a.W1, a.status, a.tmaps, s, c.px);
@@ -400,9 +478,47 @@ cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable&
   if (ev) cudaEventRecord(ev[3], s);
   return cudaGetLastError();
 }
+}  // namespace
+
+cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s,
+                               cudaEvent_t ev[4]) {
+  if (ev) cudaEventRecord(ev[0], s);
+  launch_x<false, kXLines>(a, c, q, 0, 0, s);
+  if (ev) cudaEventRecord(ev[1], s);
+  return launch_yz(a, c, s, ev);
+}
 
 cudaError_t launch_step(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s) {
   return launch_step_events(a, c, q, s, nullptr);
+}
+
+cudaError_t launch_step_scheduled(const StepArgs& a, const Coeffs& c, const DevSchedule* ds, cudaStream_t s) {
+  launch_x_sched(a, c, ds, s);
+  return launch_yz(a, c, s, nullptr);
+}
+
+cudaError_t launch_history_row(const Dims& d, const double* T, int layer, double dz2, double* hist,
+                               const DevSchedule* ds, cudaStream_t s) {
+  history_row_kernel<<<blocks(d.nxy(), 256), 256, 0, s>>>(d.nxy(), T, layer, dz2, hist, ds);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tick(DevSchedule* ds, int advance_step, cudaStream_t s) {
+  tick_kernel<<<1, 1, 0, s>>>(ds, advance_step);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_schedule_flags(const double* q, int64_t nrows, uint8_t* active, cudaStream_t s) {
+  if (nrows <= 0) return cudaSuccess;
+  schedule_flags_kernel<<<blocks(nrows, 8), 256, 0, s>>>(q, nrows, active);
+  return cudaGetLastError();
+}
+
+double surface_dz2(double dz) {
+  // dz^2 as the reference's dz**2.0 computes it: the C library's pow, which can differ from dz*dz by an ulp (the
+  // volatile exponent keeps the compiler from replacing the call by a multiplication)
+  volatile double two = 2.0;
+  return std::pow(dz, (double)two);
 }
 
 template <int LINES>
@@ -446,10 +562,7 @@ cudaError_t launch_copy_layer(const Dims& d, const double* T, int layer, double*
 }
 
 cudaError_t launch_surface_estimate(int64_t nxy, const double* T, double dz, double* dst, cudaStream_t s) {
-  // dz^2 as the reference's dz**2.0 computes it: the C library's pow, which can differ from dz*dz by an ulp (the
-  // volatile exponent keeps the compiler from replacing the call by a multiplication)
-  volatile double two = 2.0;
-  const double dz2 = std::pow(dz, (double)two);
+  const double dz2 = surface_dz2(dz);
   surface_estimate_kernel<<<blocks(nxy, 256), 256, 0, s>>>(nxy, T, dz2, dst);
   return cudaGetLastError();
 }

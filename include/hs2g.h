@@ -43,6 +43,7 @@ extern "C" {
 #define HS2G_SYNC 2              /* synchronise the handle's stream before returning */
 #define HS2G_REUSE 4             /* hs2g_source_*: use the device copy of the per-voxel array kept from the
                                     previous call for the same class (the caller's array is unchanged) */
+#define HS2G_SCHEDULED 8         /* hs2g_run: class sources from the handle's device schedule at its clock */
 
 /* material kinds (heatsim2/__init__.py:42-43) */
 #define HS2G_TEMPERATURE_COMPUTE 0
@@ -166,9 +167,17 @@ int hs2g_step(hs2g_handle* h, const double* T_in, double* T_out, const double* q
               const uint8_t* volumetric, int flags);
 
 /*
- * nsteps timesteps on the device (one CUDA graph per step shape).  qtabs is a host array
- * [nsteps][HS2G_MAX_CLASSES] of per-step class sources or NULL.  When history is not NULL, the layer
- * z = record_layer of T after every step is written to history[nsteps][ny][nx].
+ * nsteps timesteps on the device (replaces the reference's run_adi_steps loop over a run's times,
+ * alternatingdirection_c_pyx.pyx:387-416).  After the first step (queued directly when T_in != T_out) every
+ * step is one replay of a captured CUDA graph of the in-place step, whose x sweep reads the step's class
+ * sources from the handle's device schedule at the schedule clock (hs2g_set_schedule) and whose last kernel
+ * advances the clock; graphs are kept per (T buffer, history buffer, layer) and reused by later calls.
+ *   qtabs  host array [nsteps][HS2G_MAX_CLASSES] of per-step class sources: replaces the handle's schedule
+ *          (as hs2g_set_schedule with these rows, clock 0) before the steps; or NULL: with HS2G_SCHEDULED the
+ *          steps take rows from the schedule already set, from its clock on (rows past its end: no source),
+ *          and without it no class source.
+ * When history is not NULL, the layer z = record_layer of T after every step is written to
+ * history[nsteps][ny][nx].
  */
 int hs2g_run(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, const double* qtabs,
              int record_layer, double* history, int flags);
@@ -209,6 +218,19 @@ int hs2g_fp64_fma_rate(int device, double* fma_per_s);
    number of classes with a non-zero value (>= 0) or an error. */
 int hs2g_source_table(int nsrc, const int32_t* kind, const double* params, double t, double dt, double volume,
                       double* qtab);
+
+/*
+ * Device-resident source schedule of a handle (the batched form's hs2g_batch_set_sources for one problem):
+ * qtabs[nsteps][HS2G_MAX_CLASSES] class source values (W/m^3) for steps 0 .. nsteps-1, a host array or, with
+ * HS2G_DEVICE, a device array copied on the handle's stream.  Sets the clock to 0; a step reads row `clock`
+ * (none when clock >= nsteps; nsteps = 0 clears the schedule) and advances the clock.  Row values multiply the
+ * per-voxel source shapes as hs2g_step's qtab does (hs2g_source_zdecay / hs2g_source_point, as they stand when
+ * the run is queued).  Steps queued earlier on the handle's stream read the rows they were queued with.
+ */
+int hs2g_set_schedule(hs2g_handle* h, int64_t nsteps, const double* qtabs, int flags);
+/* Set the schedule clock (queued on the handle's stream), or read it (waits for the stream). */
+int hs2g_set_clock(hs2g_handle* h, int64_t step);
+int hs2g_get_clock(hs2g_handle* h, int64_t* step);
 
 /*
  * Per-voxel source shapes: the source kinds whose value differs between the voxels of a class are evaluated on
