@@ -63,7 +63,7 @@ struct hs2g_handle {
   int64_t* shape_tiles = nullptr;
   unsigned long long* err_dev = nullptr;
   int* status_dev = nullptr;
-  bool bulk_y = false, bulk_z = false;
+  bool bulk_y = false, bulk_z = false, z_discard = true;
   bool per_row = false;  // compiled from per-row conductances (hs2g_create_rows): no shared face arrays
   hs2g::TensorMapCache* tmaps = nullptr;
   int64_t bytes = 0;
@@ -234,9 +234,12 @@ int alloc_common(hs2g_handle* h, bool faces = true) {
   // tensor-tile line sweeps need 16-byte aligned coefficient arrays (an even voxel count) and even row pitches
   HS2G_CUDA(hs2g::lines_bulk_prepare(), "configure line-sweep kernels");
   // Kernel variants (defaults are the fastest measured on GB300; the others stay selectable for comparison
-  // and testing): HS2G_LINE_SWEEP=plain the plain-load y sweep, HS2G_Z_SWEEP=tma the TMA tensor-tile z sweep.
+  // and testing): HS2G_LINE_SWEEP=plain the plain-load y sweep, HS2G_Z_SWEEP=tma the TMA tensor-tile z sweep,
+  // HS2G_Z_DISCARD=0 the plain z sweep leaving its forward values to L2's own eviction.
   const char* ymode = getenv("HS2G_LINE_SWEEP");
   const char* zmode = getenv("HS2G_Z_SWEEP");
+  const char* zdiscard = getenv("HS2G_Z_DISCARD");
+  h->z_discard = !(zdiscard && strcmp(zdiscard, "0") == 0);
   h->bulk_y = !(ymode && strcmp(ymode, "plain") == 0) && hs2g::lines_bulk_supported(h->d, 1, h->c.px);
   h->bulk_z = (zmode && strcmp(zmode, "tma") == 0) && h->c.px == h->d.nx && (n % 2 == 0) &&
               hs2g::lines_bulk_supported(h->d, 2, h->d.nx);
@@ -256,6 +259,7 @@ hs2g::StepArgs make_args(const hs2g_handle* h, const double* T_in, const double*
   const bool aligned = ((reinterpret_cast<uintptr_t>(T_in) | reinterpret_cast<uintptr_t>(T_out)) & 15u) == 0;
   a.bulk_y = h->bulk_y;
   a.bulk_z = h->bulk_z && aligned;
+  a.z_discard = h->z_discard;
   a.tmaps = h->tmaps;
   return a;
 }
@@ -864,16 +868,15 @@ int set_schedule_rows(hs2g_handle* h, int64_t nsteps, const double* qtabs, bool 
   return set_clock(h, 0);
 }
 
-// One step src -> dst whose sources come from the schedule at its clock (or none), with the history row and the
-// clock tick after it, queued on stream s.
+// One step src -> dst whose sources come from the schedule at its clock (or none), with the history row after
+// it, queued on stream s; the step's x sweep advances the clock.
 cudaError_t queue_step(hs2g_handle* h, const double* src, double* dst, double* hist, int layer, double dz2,
                        bool scheduled, cudaStream_t s) {
   hs2g::StepArgs a = make_args(h, src, dst);
   a.T_in = src;
   a.T_out = dst;
-  cudaError_t e = hs2g::launch_step_scheduled(a, h->c, scheduled ? h->sched_dev : nullptr, s);
+  cudaError_t e = hs2g::launch_step_scheduled(a, h->c, h->sched_dev, scheduled, s);
   if (e == cudaSuccess && hist) e = hs2g::launch_history_row(h->d, dst, layer, dz2, hist, h->sched_dev, s);
-  if (e == cudaSuccess && (scheduled || hist)) e = hs2g::launch_tick(h->sched_dev, scheduled ? 1 : 0, s);
   return e;
 }
 
@@ -953,6 +956,8 @@ int run_steps(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, con
     }
     HS2G_CUDA(cudaMemsetAsync(&h->sched_dev->row, 0, sizeof(int64_t), s), "reset history row");
   }
+  // the finished-CTA count of the x sweep starts every call at 0 (a step that failed part-way may have left it)
+  HS2G_CUDA(cudaMemsetAsync(&h->sched_dev->ctas_done, 0, sizeof(unsigned int), s), "reset clock count");
   const int layer = hist && surface_dz <= 0.0 ? record_layer : 0;
   const double dz2 = hist && surface_dz > 0.0 ? hs2g::surface_dz2(surface_dz) : 0.0;
   int done = 0;

@@ -55,7 +55,9 @@ struct DevSchedule {
   int64_t n;               // rows; steps at or beyond n have no source
   int64_t step;
   int64_t row;
+  unsigned int ctas_done;  // x-sweep CTAs of the current step that have finished (the last one advances the clock)
 };
+
 
 // Record the message hs2g_last_error() returns for this thread (hs2g_api.cu); returns code.
 int set_last_error(int code, const char* message);
@@ -107,6 +109,7 @@ struct StepArgs {
   bool has_qtab;
   int* status;           // device word: 0, or HS2G_ERR_TIMEOUT when a bounded wait in a kernel ran out
   bool bulk_y, bulk_z;   // use the TMA tensor-tile line sweeps (hs2g_lines.cu) for y / z
+  bool z_discard;        // the plain z sweep drops its forward values from L2 after reading them
   struct TensorMapCache* tmaps;
 };
 
@@ -124,15 +127,15 @@ cudaError_t launch_step(const StepArgs& a, const Coeffs& c, const QTable& q, cud
 // the same three kernels with an event recorded before each and after the last (ev[0..3])
 cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s,
                                cudaEvent_t ev[4]);
-// One step whose class sources come from the device schedule ds at its clock (ds null: no source); the x sweep
-// decides on the device whether the step has a source.  Used for the captured step graph of hs2g_run.
-cudaError_t launch_step_scheduled(const StepArgs& a, const Coeffs& c, const DevSchedule* ds, cudaStream_t s);
-// History of the step just taken into hist[ds->row][ny][nx]: layer `layer` of T (dz2 <= 0) or the insulating
-// z = 0 surface estimate from layers 0 and 1 with dz2 = dz**2 (dz2 > 0).
+// One step for the captured step graph of hs2g_run.  With use_schedule the class sources come from the device
+// schedule ds at its clock (the x sweep decides on the device whether the step has a source), otherwise there
+// is none; the x sweep's last CTA advances ds->row, and ds->step with use_schedule.
+cudaError_t launch_step_scheduled(const StepArgs& a, const Coeffs& c, DevSchedule* ds, bool use_schedule,
+                                  cudaStream_t s);
+// History of the step just taken into hist[ds->row - 1][ny][nx] (the x sweep has advanced the row): layer `layer`
+// of T (dz2 <= 0) or the insulating z = 0 surface estimate from layers 0 and 1 with dz2 = dz**2 (dz2 > 0).
 cudaError_t launch_history_row(const Dims& d, const double* T, int layer, double dz2, double* hist,
                                const DevSchedule* ds, cudaStream_t s);
-// Advance the schedule clock after a step: row += 1, and step += 1 when advance_step.
-cudaError_t launch_tick(DevSchedule* ds, int advance_step, cudaStream_t s);
 // the reference's dz**2.0 (the C library's pow)
 double surface_dz2(double dz);
 // one flag per schedule row: active[s] = any of q[s][0..nclass-1] non-zero

@@ -29,7 +29,6 @@ constexpr int kXLines = 32;   // x-lines per CTA
 constexpr int kXChunk = 32;   // columns per staged chunk
 constexpr int kXThreads = 128;
 constexpr int kXWarps = kXThreads / 32;
-constexpr int kXLinesPerWarp = kXLines / kXWarps;
 // Register budget of the x sweep: at 72 registers 7 CTAs of 128 threads fit on an SM, so the 1040 CTAs of a
 // 65 x 512-line grid run in one wave on 152 SMs with the most loads in flight per thread (332 us at
 // 65x512x512; 80 registers: 6 CTAs per SM and a second wave, 530 us; the compiler's own choice of 48
@@ -234,32 +233,47 @@ __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d,
                                         sa, sq);
 }
 
-// The x sweep of a scheduled step (the captured step graph of hs2g_run): the class table is row ds->step of the
-// handle's device schedule, read here, and the CTA takes the source body or the plain one by the row's flag, so
-// one launch serves the steps with and without a source.  Both bodies share the kernel's shared arrays.
+// The x sweep of a scheduled step (the captured step graph of hs2g_run): with use_schedule the class table is
+// row ds->step of the handle's device schedule, and the CTA takes the source body or the plain one by the row's
+// flag, so one launch serves the steps with and without a source (both bodies share the kernel's shared
+// arrays).  Every CTA reads the clock at its start; the last CTA to finish advances it (row, and step with
+// use_schedule) after counting the finished CTAs, so the next kernels and the next step see the new values.
 template <int PITCH>
 __global__ void __maxnreg__(72) sweep_x_sched_kernel(Dims d, const double* __restrict__ T, Coeffs c,
-                                                     const uint8_t* __restrict__ vclass,
-                                                     const DevSchedule* __restrict__ ds, double* __restrict__ W0) {
+                                                     const uint8_t* __restrict__ vclass, DevSchedule* ds,
+                                                     int use_schedule, double* __restrict__ W0) {
   __shared__ double sr[kXLines][kXChunk + 1];
   __shared__ double sa[kXLines][kXChunk + 1];
   __shared__ double sq[HS2G_MAX_CLASSES];
-  const double* qrow = nullptr;
-  const double* shape = nullptr;
-  if (ds) {
-    const int64_t st = ds->step;
-    if (st >= 0 && st < ds->n && ds->active[st]) {
-      qrow = ds->q + st * HS2G_MAX_CLASSES;
-      shape = ds->shape;
+  __shared__ const double* s_row;
+  __shared__ const double* s_shape;
+  if (threadIdx.x == 0) {
+    const double* row = nullptr;
+    if (use_schedule) {
+      const int64_t st = *(volatile int64_t*)&ds->step;
+      if (st >= 0 && st < ds->n && ds->active[st]) row = ds->q + st * HS2G_MAX_CLASSES;
     }
+    s_row = row;
+    s_shape = ds->shape;
   }
+  __syncthreads();
+  const double* qrow = s_row;
   const int no_table = 0;  // the table comes from qrow
   if (qrow)
-    sweep_x_body<true, false, kXLines, PITCH, true>(d, T, c, vclass, nullptr, shape, no_table, qrow, W0, 0, 0, sr,
+    sweep_x_body<true, false, kXLines, PITCH, true>(d, T, c, vclass, nullptr, s_shape, no_table, qrow, W0, 0, 0, sr,
                                                     sa, sq);
   else
     sweep_x_body<false, false, kXLines, PITCH, true>(d, T, c, vclass, nullptr, nullptr, no_table, nullptr, W0, 0, 0,
                                                      sr, sa, sq);
+  if (threadIdx.x == 0) {  // the body ends with a barrier: every thread of the CTA is done with the clock
+    __threadfence();
+    if (atomicAdd(&ds->ctas_done, 1u) == gridDim.x - 1) {
+      ds->row += 1;
+      if (use_schedule) ds->step += 1;
+      ds->ctas_done = 0;
+      __threadfence();
+    }
+  }
 }
 
 // x sweep over all lines (RANGED false) or the lines [line_begin, line_end) of the host-buffer step
@@ -297,16 +311,16 @@ void launch_x(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_
 #undef HS2G_X
 }
 
-void launch_x_sched(const StepArgs& a, const Coeffs& c, const DevSchedule* ds, cudaStream_t s) {
+void launch_x_sched(const StepArgs& a, const Coeffs& c, DevSchedule* ds, int use_schedule, cudaStream_t s) {
   const Dims& d = a.d;
   const unsigned gx = (unsigned)((d.nz * d.ny + kXLines - 1) / kXLines);
   const int pitch = c.px == d.nx ? 0 : c.px == d.nx + 1 ? 1 : 2;
   if (pitch == 0)
-    sweep_x_sched_kernel<0><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, a.W0);
+    sweep_x_sched_kernel<0><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, use_schedule, a.W0);
   else if (pitch == 1)
-    sweep_x_sched_kernel<1><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, a.W0);
+    sweep_x_sched_kernel<1><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, use_schedule, a.W0);
   else
-    sweep_x_sched_kernel<2><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, a.W0);
+    sweep_x_sched_kernel<2><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, use_schedule, a.W0);
 }
 
 // y lines: W1 = s2 * dT1 from W0 = sigma * dT0
@@ -333,9 +347,21 @@ __global__ void __launch_bounds__(kLineThreads) sweep_y_kernel(Dims d, const dou
   }
 }
 
+// Drop a 128-byte L2 line without writing it back: its contents become undefined until written again.
+__device__ __forceinline__ void discard_line(const double* p) {
+  asm volatile("discard.global.L2 [%0], 128;" ::"l"(p) : "memory");
+}
+
 // z lines: dT2 from W1 = s2 * dT1; T_out = T_in + dT2.  Z is scratch (the x sweep's buffer, free by now).
 // T_in may equal T_out: each voxel's T_in is read by the same thread just before its T_out is written.
-__global__ void __launch_bounds__(kLineThreads) sweep_z_kernel(Dims d, const double* __restrict__ W1,
+// DISCARD: the forward values are read once by the back substitution and never again, so once a warp has read
+// a group of 4 rows k .. k+3 (k a multiple of 4) it drops their Z lines from L2 (lanes 0 and 16 each own one
+// 128-byte line of a row), which saves the write-back of every line still cached; only warps whose 32 columns
+// are whole lines of every plane do this (nxy a multiple of 16, warp-aligned columns inside the launch's range),
+// and the rows above the top group (nz mod 4 of them) are left as they are.
+// 16 CTAs per SM (32 registers): the 2048 CTAs of a 512x512-column grid are resident at once.
+template <bool DISCARD>
+__global__ void __launch_bounds__(kLineThreads, 16) sweep_z_kernel(Dims d, const double* __restrict__ W1,
                                                                 const double* __restrict__ a2,
                                                                 const double* __restrict__ b2, const double* T_in,
                                                                 double* __restrict__ Z, double* T_out,
@@ -343,6 +369,8 @@ __global__ void __launch_bounds__(kLineThreads) sweep_z_kernel(Dims d, const dou
   // this launch covers the z-lines (columns j*nx + i) [col_begin, col_end); W1 has row pitch px
   const int64_t t = col_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nxy = d.nxy();
+  const int64_t t0 = t - (threadIdx.x & 31);  // the warp's first column
+  const bool drop = DISCARD && nxy % 16 == 0 && t0 % 32 == 0 && t0 + 32 <= col_end;  // warp-uniform
   if (t >= col_end) return;
   int64_t p = t;
   const int64_t jw = t / d.nx;
@@ -356,11 +384,42 @@ __global__ void __launch_bounds__(kLineThreads) sweep_z_kernel(Dims d, const dou
     st_keep(Z + p, z, keep);
   }
   double x = 0.0;
+  if (!DISCARD) {
 #pragma unroll 4
-  for (int64_t k = d.nz - 1; k >= 0; --k) {
+    for (int64_t k = d.nz - 1; k >= 0; --k) {
+      p -= nxy;
+      x = fma(-b2[p], x, Z[p]);
+      T_out[p] = T_in[p] + x;
+    }
+    return;
+  }
+  int64_t k = d.nz - 1;
+#pragma unroll 1
+  for (; (k & 3) != 3; --k) {  // rows above the last whole group of 4
     p -= nxy;
     x = fma(-b2[p], x, Z[p]);
     T_out[p] = T_in[p] + x;
+  }
+#pragma unroll 1
+  for (; k >= 3; k -= 4) {  // rows k-3 .. k, then their Z lines dropped
+    p -= 4 * nxy;
+    double z3 = Z[p + 3 * nxy], z2 = Z[p + 2 * nxy], z1 = Z[p + nxy], z0 = Z[p];
+    x = fma(-b2[p + 3 * nxy], x, z3);
+    T_out[p + 3 * nxy] = T_in[p + 3 * nxy] + x;
+    x = fma(-b2[p + 2 * nxy], x, z2);
+    T_out[p + 2 * nxy] = T_in[p + 2 * nxy] + x;
+    x = fma(-b2[p + nxy], x, z1);
+    T_out[p + nxy] = T_in[p + nxy] + x;
+    x = fma(-b2[p], x, z0);
+    T_out[p] = T_in[p] + x;
+    if (!drop) continue;
+    __syncwarp();  // every lane of the warp has read its four rows of Z
+    if ((threadIdx.x & 15) == 0) {
+      discard_line(Z + p);
+      discard_line(Z + p + nxy);
+      discard_line(Z + p + 2 * nxy);
+      discard_line(Z + p + 3 * nxy);
+    }
   }
 }
 
@@ -386,19 +445,14 @@ __global__ void surface_estimate_kernel(int64_t nxy, const double* __restrict__ 
 }
 
 inline unsigned blocks(int64_t n, int per) { return (unsigned)((n + per - 1) / per); }
-// History of a scheduled step into row ds->row of hist: layer `layer` of T, or (dz2 > 0) the surface estimate.
+// History of a scheduled step into row ds->row - 1 of hist (the step's x sweep advanced the row): layer `layer`
+// of T, or (dz2 > 0) the surface estimate.
 __global__ void history_row_kernel(int64_t nxy, const double* __restrict__ T, int layer, double dz2,
                                    double* __restrict__ hist, const DevSchedule* __restrict__ ds) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= nxy) return;
-  double* dst = hist + ds->row * nxy;
+  double* dst = hist + (ds->row - 1) * nxy;
   dst[t] = dz2 > 0.0 ? surface_value(T[t], T[nxy + t], dz2) : T[(int64_t)layer * nxy + t];
-}
-
-// The last node of a scheduled step: every kernel of the step that reads the clock has completed.
-__global__ void tick_kernel(DevSchedule* ds, int advance_step) {
-  ds->row += 1;
-  if (advance_step) ds->step += 1;
 }
 
 __global__ void schedule_flags_kernel(const double* __restrict__ q, int64_t nrows, uint8_t* __restrict__ active) {
@@ -492,19 +546,15 @@ cudaError_t launch_step(const StepArgs& a, const Coeffs& c, const QTable& q, cud
   return launch_step_events(a, c, q, s, nullptr);
 }
 
-cudaError_t launch_step_scheduled(const StepArgs& a, const Coeffs& c, const DevSchedule* ds, cudaStream_t s) {
-  launch_x_sched(a, c, ds, s);
+cudaError_t launch_step_scheduled(const StepArgs& a, const Coeffs& c, DevSchedule* ds, bool use_schedule,
+                                  cudaStream_t s) {
+  launch_x_sched(a, c, ds, use_schedule ? 1 : 0, s);
   return launch_yz(a, c, s, nullptr);
 }
 
 cudaError_t launch_history_row(const Dims& d, const double* T, int layer, double dz2, double* hist,
                                const DevSchedule* ds, cudaStream_t s) {
   history_row_kernel<<<blocks(d.nxy(), 256), 256, 0, s>>>(d.nxy(), T, layer, dz2, hist, ds);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_tick(DevSchedule* ds, int advance_step, cudaStream_t s) {
-  tick_kernel<<<1, 1, 0, s>>>(ds, advance_step);
   return cudaGetLastError();
 }
 
@@ -550,9 +600,13 @@ cudaError_t launch_y(const StepArgs& a, const Coeffs& c, cudaStream_t s) {
 cudaError_t launch_z_range(const StepArgs& a, const Coeffs& c, int64_t col_begin, int64_t col_end, cudaStream_t s) {
   const Dims& d = a.d;
   if (col_end <= col_begin) return cudaSuccess;
-  sweep_z_kernel<<<blocks(col_end - col_begin, kLineThreads), kLineThreads, 0, s>>>(d, a.W1, c.a2, c.b2, a.T_in,
-                                                                                     a.W0, a.T_out, col_begin,
-                                                                                     col_end, c.px);
+  const unsigned grid = blocks(col_end - col_begin, kLineThreads);
+  if (a.z_discard)
+    sweep_z_kernel<true><<<grid, kLineThreads, 0, s>>>(d, a.W1, c.a2, c.b2, a.T_in, a.W0, a.T_out, col_begin, col_end,
+                                                        c.px);
+  else
+    sweep_z_kernel<false><<<grid, kLineThreads, 0, s>>>(d, a.W1, c.a2, c.b2, a.T_in, a.W0, a.T_out, col_begin,
+                                                         col_end, c.px);
   return cudaGetLastError();
 }
 

@@ -138,19 +138,22 @@ def test_composite_panel_midsize_vs_oracle(cuda_ok):
     _compare_with_oracle(spec, 25)
 
 
-@pytest.mark.parametrize("shape", [(20, 70, 66), (9, 33, 41)])
+@pytest.mark.parametrize("shape", [(20, 70, 66), (9, 33, 41), (13, 48, 80)])
 def test_sweep_kernel_variants_agree_bitwise(cuda_ok, monkeypatch, shape):
     """Every selectable sweep kernel does the same FMAs in the same order, so the results are identical: TMA
-    bulk-copy or plain-load y / z sweeps, and the y sweep's arrays unpadded (even nx) or padded to a row pitch
-    of 64 (odd nx always gets one pad column, so that the TMA sweep applies)."""
+    bulk-copy or plain-load y / z sweeps, the plain z sweep with or without dropping its forward values from
+    L2 (planes of a multiple of 16 voxels, as 48x80, let whole warps drop them), and the y sweep's arrays
+    unpadded (even nx) or padded to a row pitch of 64 (odd nx always gets one pad column, so that the TMA sweep
+    applies)."""
     nz, ny, nx = shape
     spec = W.composite_panel(seed=5, nz=nz, ny=ny, nx=nx, top_layers=4, width_range=(5, 20), depth_range=(2, 6))
     outs = []
-    variants = (("tma", "plain", "2"), ("plain", "tma", "2"), ("plain", "plain", "2"), ("tma", "plain", "64"),
-                ("plain", "plain", "64"))
-    for y_mode, z_mode, pitch in variants:
+    variants = (("tma", "plain", "2", "1"), ("plain", "tma", "2", "1"), ("plain", "plain", "2", "1"),
+                ("tma", "plain", "64", "1"), ("plain", "plain", "64", "1"), ("tma", "plain", "2", "0"))
+    for y_mode, z_mode, pitch, discard in variants:
         monkeypatch.setenv("HS2G_LINE_SWEEP", y_mode)
         monkeypatch.setenv("HS2G_Z_SWEEP", z_mode)
+        monkeypatch.setenv("HS2G_Z_DISCARD", discard)
         monkeypatch.setenv("HS2G_ROW_PITCH", pitch)   # rows of the y-sweep arrays padded to this multiple
         P, S = _setup(spec)
         outs.append(_run_host(spec, W.step_times(spec, 5), P, S)[5])
