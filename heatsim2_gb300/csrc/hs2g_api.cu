@@ -1,5 +1,6 @@
 // C ABI of the hs2g library (declared in include/hs2g.h).  Host-side runtime: owns device buffers, compiles a
 // problem into step coefficients and queues timesteps on a stream.
+#include <algorithm>
 #include <cmath>
 #include <cstddef>
 #include <cstdarg>
@@ -72,11 +73,15 @@ struct hs2g_handle {
   cudaStream_t copy_stream = nullptr;
   cudaStream_t x_stream[kCopyChunks] = {};
   cudaEvent_t ev_in[kCopyChunks] = {}, ev_x[kCopyChunks] = {}, ev_out[kCopyChunks] = {}, ev_begin = nullptr;
-  // device source schedule (hs2g_set_schedule): the descriptor the scheduled x sweep reads, its rows and flags
+  // device source schedule (hs2g_set_schedule): the descriptor the x sweep of a step with a source reads, the
+  // rows and their flags on the device, the flags mirrored on the host (which steps have a source), and the
+  // clock (the schedule row of the next scheduled step)
   hs2g::DevSchedule* sched_dev = nullptr;
   double* sched_q = nullptr;
   uint8_t* sched_active = nullptr;
   int64_t sched_cap = 0, sched_n = 0;
+  std::vector<uint8_t> sched_flags;
+  int64_t clock = 0;
   // captured in-place step graphs of hs2g_run, keyed by what they bake in; captured on a stream of their own
   // (capture is not allowed on the legacy default stream the caller may have chosen) and launched on `stream`
   struct StepGraph {
@@ -84,7 +89,8 @@ struct hs2g_handle {
     double* hist;
     int layer;
     double dz2;
-    bool scheduled;
+    bool source;  // one step whose x sweep reads its row of the schedule; else `steps` steps without a source
+    int steps;
     cudaGraphExec_t exec;
   };
   std::vector<StepGraph> graphs;
@@ -822,14 +828,13 @@ int ensure_schedule(hs2g_handle* h) {
   return HS2G_OK;
 }
 
-// Queue the host-owned fields of the schedule descriptor (rows, flags, row count, shape field) on the handle's
-// stream; the clock fields are left as they are.  The descriptor names the shape field only while some class has
-// a shape: a voxel's class value is multiplied by its shape value, which is 1 for every voxel of a class without
-// one, so the product is exact for those classes.
+// Queue the schedule descriptor's rows, flags, row count and shape field on the handle's stream.  The
+// descriptor names the shape field only while some class has a shape: a voxel's class value is multiplied by
+// its shape value, which is 1 for every voxel of a class without one, so the product is exact for those classes.
 int write_schedule_header(hs2g_handle* h) {
   bool any_shape = false;
   for (int c = 0; c < HS2G_MAX_CLASSES && h->qshape; ++c) any_shape |= h->shaped[c];
-  const hs2g::DevSchedule hdr{h->sched_q, h->sched_active, any_shape ? h->qshape : nullptr, h->sched_n, 0, 0};
+  const hs2g::DevSchedule hdr{h->sched_q, h->sched_active, any_shape ? h->qshape : nullptr, h->sched_n, 0, 0, 0};
   // a pageable source is staged before the call returns, so the local descriptor may go out of scope
   HS2G_CUDA(cudaMemcpyAsync(h->sched_dev, &hdr, offsetof(hs2g::DevSchedule, step), cudaMemcpyHostToDevice,
                             h->stream),
@@ -837,14 +842,10 @@ int write_schedule_header(hs2g_handle* h) {
   return HS2G_OK;
 }
 
-int set_clock(hs2g_handle* h, int64_t step) {
-  HS2G_CUDA(cudaMemcpyAsync(&h->sched_dev->step, &step, sizeof(step), cudaMemcpyHostToDevice, h->stream),
-            "set schedule clock");
-  return HS2G_OK;
-}
-
 // Replace the schedule's rows by qtabs[nsteps][HS2G_MAX_CLASSES] (host, or device when device_ptr) and set the
-// clock to 0.  Work already queued on the handle's stream reads the old rows before they are overwritten.
+// clock to 0.  Work already queued on the handle's stream reads the old rows before they are overwritten.  The
+// flags (row has a non-zero value) are computed on the device and mirrored on the host, which picks each step's
+// graph from them.
 int set_schedule_rows(hs2g_handle* h, int64_t nsteps, const double* qtabs, bool device_ptr) {
   int rc = ensure_schedule(h);
   if (rc) return rc;
@@ -857,42 +858,58 @@ int set_schedule_rows(hs2g_handle* h, int64_t nsteps, const double* qtabs, bool 
     if ((rc = dalloc(h, &h->sched_active, nsteps, "source schedule flags"))) return rc;
     h->sched_cap = nsteps;
   }
+  h->sched_flags.assign((size_t)nsteps, 0);
   if (nsteps > 0) {
     HS2G_CUDA(cudaMemcpyAsync(h->sched_q, qtabs, sizeof(double) * HS2G_MAX_CLASSES * (size_t)nsteps,
                               device_ptr ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream),
               "upload source schedule");
     HS2G_CUDA(hs2g::launch_schedule_flags(h->sched_q, nsteps, h->sched_active, h->stream), "schedule flags");
+    HS2G_CUDA(cudaMemcpyAsync(h->sched_flags.data(), h->sched_active, (size_t)nsteps, cudaMemcpyDeviceToHost,
+                              h->stream),
+              "read schedule flags");
+    HS2G_CUDA(cudaStreamSynchronize(h->stream), "source schedule");
   }
   h->sched_n = nsteps;
-  if ((rc = write_schedule_header(h))) return rc;
-  return set_clock(h, 0);
+  h->clock = 0;
+  return write_schedule_header(h);
 }
 
-// One step src -> dst whose sources come from the schedule at its clock (or none), with the history row after
-// it, queued on stream s; the step's x sweep advances the clock.
+// One step src -> dst queued on s: with `source`, the x sweep whose class table is the schedule's row at the
+// device clock (set by the caller), else the x sweep without a source; then y, z and the history row.
 cudaError_t queue_step(hs2g_handle* h, const double* src, double* dst, double* hist, int layer, double dz2,
-                       bool scheduled, cudaStream_t s) {
+                       bool source, cudaStream_t s) {
   hs2g::StepArgs a = make_args(h, src, dst);
   a.T_in = src;
   a.T_out = dst;
-  cudaError_t e = hs2g::launch_step_scheduled(a, h->c, h->sched_dev, scheduled, s);
+  cudaError_t e;
+  if (source) {
+    e = hs2g::launch_step_row(a, h->c, h->sched_dev, s);
+  } else {
+    hs2g::QTable q;
+    memset(&q, 0, sizeof(q));
+    a.has_qtab = false;
+    e = hs2g::launch_step(a, h->c, q, s);
+  }
   if (e == cudaSuccess && hist) e = hs2g::launch_history_row(h->d, dst, layer, dz2, hist, h->sched_dev, s);
   return e;
 }
 
-// The captured in-place step on T (T_in == T_out == T), from the handle's cache or captured now.
+// The captured in-place steps on T (T_in == T_out == T): one step with a source, or `steps` without; from the
+// handle's cache or captured now.
 constexpr size_t kMaxStepGraphs = 8;
-int step_graph(hs2g_handle* h, double* T, double* hist, int layer, double dz2, bool scheduled,
+int step_graph(hs2g_handle* h, double* T, double* hist, int layer, double dz2, bool source, int steps,
                cudaGraphExec_t* out) {
   for (const auto& g : h->graphs)
-    if (g.T == T && g.hist == hist && g.layer == layer && g.dz2 == dz2 && g.scheduled == scheduled) {
+    if (g.T == T && g.hist == hist && g.layer == layer && g.dz2 == dz2 && g.source == source && g.steps == steps) {
       *out = g.exec;
       return HS2G_OK;
     }
   if (!h->cap_stream)
     HS2G_CUDA(cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking), "capture stream");
   HS2G_CUDA(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal), "begin step capture");
-  cudaError_t e = queue_step(h, T, T, hist, layer, dz2, scheduled, h->cap_stream);
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < steps && e == cudaSuccess; ++k)
+    e = queue_step(h, T, T, hist, layer, dz2, source, h->cap_stream);
   cudaGraph_t g = nullptr;
   const cudaError_t e_end = cudaStreamEndCapture(h->cap_stream, &g);
   if (e == cudaSuccess) e = e_end;
@@ -907,14 +924,21 @@ int step_graph(hs2g_handle* h, double* T, double* hist, int layer, double dz2, b
     cudaGraphExecDestroy(h->graphs.front().exec);
     h->graphs.erase(h->graphs.begin());
   }
-  h->graphs.push_back({T, hist, layer, dz2, scheduled, exec});
+  h->graphs.push_back({T, hist, layer, dz2, source, steps, exec});
   *out = exec;
   return HS2G_OK;
 }
 
+// Steps without a source are replayed kStepsPerGraph at a time: the boundary between two graph launches costs
+// about 3 us more than one between kernels of a graph (0.5777 against 0.5810 ms per step at 65x512x512; 16
+// steps per graph measured the same as 4).
+constexpr int kStepsPerGraph = 4;
+
 // hs2g_run and hs2g_run_surface: after every step, history receives layer record_layer of T, or (surface_dz > 0)
 // the insulating z = 0 surface temperature estimated from layers 0 and 1.  The first step of a call with
-// T_in != T_out is queued directly; every further step is one replay of the captured in-place step graph.
+// T_in != T_out is queued directly; the others are replays of captured in-place step graphs.  A scheduled
+// step whose row has a source writes the clock to the descriptor and replays the one-step source graph; runs
+// of steps without one replay the plain graphs.
 int run_steps(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, const double* qtabs, int record_layer,
               double surface_dz, double* history, int flags) {
   DeviceGuard g(h->device);
@@ -954,23 +978,51 @@ int run_steps(hs2g_handle* h, int nsteps, const double* T_in, double* T_out, con
       }
       hist = h->hist_dev;
     }
-    HS2G_CUDA(cudaMemsetAsync(&h->sched_dev->row, 0, sizeof(int64_t), s), "reset history row");
+    // the history row and the count of the history kernel's finished CTAs start at 0
+    HS2G_CUDA(cudaMemsetAsync(&h->sched_dev->row, 0, sizeof(int64_t) + sizeof(unsigned int), s),
+              "reset history row");
   }
-  // the finished-CTA count of the x sweep starts every call at 0 (a step that failed part-way may have left it)
-  HS2G_CUDA(cudaMemsetAsync(&h->sched_dev->ctas_done, 0, sizeof(unsigned int), s), "reset clock count");
   const int layer = hist && surface_dz <= 0.0 ? record_layer : 0;
   const double dz2 = hist && surface_dz > 0.0 ? hs2g::surface_dz2(surface_dz) : 0.0;
+  // whether scheduled step `i` of this call has a source, and queueing one such step (its row set first)
+  auto has_source = [&](int i) {
+    const int64_t st = h->clock + i;
+    return scheduled && st < h->sched_n && h->sched_flags[(size_t)st] != 0;
+  };
+  auto set_row = [&](int i) {
+    const int64_t st = h->clock + i;
+    return cudaMemcpyAsync(&h->sched_dev->step, &st, sizeof(st), cudaMemcpyHostToDevice, s);
+  };
   int done = 0;
   if (nsteps > 0 && src != dst) {
-    cudaError_t e = queue_step(h, src, dst, hist, layer, dz2, scheduled, s);
+    const bool source = has_source(0);
+    cudaError_t e = source ? set_row(0) : cudaSuccess;
+    if (e == cudaSuccess) e = queue_step(h, src, dst, hist, layer, dz2, source, s);
     if (e != cudaSuccess) return cuda_fail(e, "step kernels");
     done = 1;
   }
-  if (done < nsteps) {
+  while (done < nsteps) {
     cudaGraphExec_t graph = nullptr;
-    if ((rc = step_graph(h, dst, hist, layer, dz2, scheduled, &graph))) return rc;
-    for (; done < nsteps; ++done) HS2G_CUDA(cudaGraphLaunch(graph, s), "step graph");
+    if (has_source(done)) {
+      HS2G_CUDA(set_row(done), "set schedule row");
+      if ((rc = step_graph(h, dst, hist, layer, dz2, true, 1, &graph))) return rc;
+      HS2G_CUDA(cudaGraphLaunch(graph, s), "step graph");
+      ++done;
+      continue;
+    }
+    int idle = 1;  // steps without a source from here on
+    while (done + idle < nsteps && !has_source(done + idle)) ++idle;
+    if (idle >= kStepsPerGraph) {
+      if ((rc = step_graph(h, dst, hist, layer, dz2, false, kStepsPerGraph, &graph))) return rc;
+      for (; idle >= kStepsPerGraph; idle -= kStepsPerGraph, done += kStepsPerGraph)
+        HS2G_CUDA(cudaGraphLaunch(graph, s), "step graph");
+    }
+    if (idle > 0) {
+      if ((rc = step_graph(h, dst, hist, layer, dz2, false, 1, &graph))) return rc;
+      for (; idle > 0; --idle, ++done) HS2G_CUDA(cudaGraphLaunch(graph, s), "step graph");
+    }
   }
+  if (scheduled) h->clock += nsteps;
   if (nsteps == 0 && src != dst) {
     HS2G_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, s), "copy T");
   }
@@ -1001,21 +1053,13 @@ int hs2g_set_schedule(hs2g_handle* h, int64_t nsteps, const double* qtabs, int f
 
 int hs2g_set_clock(hs2g_handle* h, int64_t step) {
   if (!h || step < 0) return fail(HS2G_ERR_ARG, "hs2g_set_clock: bad argument");
-  DeviceGuard g(h->device);
-  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", h->device);
-  int rc = ensure_schedule(h);
-  return rc ? rc : set_clock(h, step);
+  h->clock = step;
+  return HS2G_OK;
 }
 
 int hs2g_get_clock(hs2g_handle* h, int64_t* step) {
   if (!h || !step) return fail(HS2G_ERR_ARG, "hs2g_get_clock: bad argument");
-  DeviceGuard g(h->device);
-  if (!g.ok) return fail(HS2G_ERR_CUDA, "cannot select device %d", h->device);
-  int rc = ensure_schedule(h);
-  if (rc) return rc;
-  HS2G_CUDA(cudaMemcpyAsync(step, &h->sched_dev->step, sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream),
-            "read schedule clock");
-  HS2G_CUDA(cudaStreamSynchronize(h->stream), "read schedule clock");
+  *step = h->clock;
   return HS2G_OK;
 }
 

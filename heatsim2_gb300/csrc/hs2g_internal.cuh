@@ -44,10 +44,10 @@ struct QTable {
   double q[HS2G_MAX_CLASSES];
 };
 
-// Device-resident source schedule of a handle, read by the scheduled x sweep at the start of every step.  The
-// first four fields are written by the host when the schedule or the source shapes change; `step` (the
-// schedule row of the next step) and `row` (the history row of the next step of the current run) are advanced
-// on the device by the step's last kernel, so that one captured step graph replays any number of steps.
+// Device-resident source schedule of a handle, read by the x sweep of a step with a source.  The host writes
+// every field: the rows, their flags and the shape field when the schedule or the shapes change, `step` (the
+// row of the next step with a source) before such a step is queued, `row` (the history row of the next step)
+// at the start of a run; the history kernel then advances `row` after each step.
 struct DevSchedule {
   const double* q;         // [n][HS2G_MAX_CLASSES] class source values (W/m^3)
   const uint8_t* active;   // [n] 1 when row s has a non-zero value
@@ -55,9 +55,8 @@ struct DevSchedule {
   int64_t n;               // rows; steps at or beyond n have no source
   int64_t step;
   int64_t row;
-  unsigned int ctas_done;  // x-sweep CTAs of the current step that have finished (the last one advances the clock)
+  unsigned int hist_done;  // CTAs of the current history kernel that have finished (the last one advances row)
 };
-
 
 // Record the message hs2g_last_error() returns for this thread (hs2g_api.cu); returns code.
 int set_last_error(int code, const char* message);
@@ -127,15 +126,15 @@ cudaError_t launch_step(const StepArgs& a, const Coeffs& c, const QTable& q, cud
 // the same three kernels with an event recorded before each and after the last (ev[0..3])
 cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s,
                                cudaEvent_t ev[4]);
-// One step for the captured step graph of hs2g_run.  With use_schedule the class sources come from the device
-// schedule ds at its clock (the x sweep decides on the device whether the step has a source), otherwise there
-// is none; the x sweep's last CTA advances ds->row, and ds->step with use_schedule.
-cudaError_t launch_step_scheduled(const StepArgs& a, const Coeffs& c, DevSchedule* ds, bool use_schedule,
-                                  cudaStream_t s);
-// History of the step just taken into hist[ds->row - 1][ny][nx] (the x sweep has advanced the row): layer `layer`
-// of T (dz2 <= 0) or the insulating z = 0 surface estimate from layers 0 and 1 with dz2 = dz**2 (dz2 > 0).
-cudaError_t launch_history_row(const Dims& d, const double* T, int layer, double dz2, double* hist,
-                               const DevSchedule* ds, cudaStream_t s);
+// One step whose class sources are row ds->step of the device schedule (no source when that row is inactive or
+// past the schedule's end): the x sweep reads the row on the device.  Used for the steps with a source in the
+// captured step graphs of hs2g_run; the steps without one use launch_step with no table.
+cudaError_t launch_step_row(const StepArgs& a, const Coeffs& c, const DevSchedule* ds, cudaStream_t s);
+// History of the step just taken into hist[ds->row][ny][nx]: layer `layer` of T (dz2 <= 0) or the insulating
+// z = 0 surface estimate from layers 0 and 1 with dz2 = dz**2 (dz2 > 0); the kernel's last CTA advances
+// ds->row.
+cudaError_t launch_history_row(const Dims& d, const double* T, int layer, double dz2, double* hist, DevSchedule* ds,
+                               cudaStream_t s);
 // the reference's dz**2.0 (the C library's pow)
 double surface_dz2(double dz);
 // one flag per schedule row: active[s] = any of q[s][0..nclass-1] non-zero

@@ -233,47 +233,28 @@ __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d,
                                         sa, sq);
 }
 
-// The x sweep of a scheduled step (the captured step graph of hs2g_run): with use_schedule the class table is
-// row ds->step of the handle's device schedule, and the CTA takes the source body or the plain one by the row's
-// flag, so one launch serves the steps with and without a source (both bodies share the kernel's shared
-// arrays).  Every CTA reads the clock at its start; the last CTA to finish advances it (row, and step with
-// use_schedule) after counting the finished CTAs, so the next kernels and the next step see the new values.
+// The x sweep of a step whose class table is row ds->step of the handle's device schedule (the steps with a
+// source in the captured step graphs of hs2g_run): thread 0 reads the row's address once for the CTA; an
+// inactive row or one past the schedule's end gives the zero table.  Only the source body is compiled here:
+// the steps without a source run sweep_x_lean_kernel, whose code a second body in the same kernel would slow
+// (measured 3 us per step at 65x512x512).
+__device__ const double kZeroRow[HS2G_MAX_CLASSES] = {};
 template <int PITCH>
-__global__ void __maxnreg__(72) sweep_x_sched_kernel(Dims d, const double* __restrict__ T, Coeffs c,
-                                                     const uint8_t* __restrict__ vclass, DevSchedule* ds,
-                                                     int use_schedule, double* __restrict__ W0) {
+__global__ void __maxnreg__(72) sweep_x_row_kernel(Dims d, const double* __restrict__ T, Coeffs c,
+                                                   const uint8_t* __restrict__ vclass,
+                                                   const DevSchedule* __restrict__ ds, double* __restrict__ W0) {
   __shared__ double sr[kXLines][kXChunk + 1];
   __shared__ double sa[kXLines][kXChunk + 1];
   __shared__ double sq[HS2G_MAX_CLASSES];
   __shared__ const double* s_row;
-  __shared__ const double* s_shape;
   if (threadIdx.x == 0) {
-    const double* row = nullptr;
-    if (use_schedule) {
-      const int64_t st = *(volatile int64_t*)&ds->step;
-      if (st >= 0 && st < ds->n && ds->active[st]) row = ds->q + st * HS2G_MAX_CLASSES;
-    }
-    s_row = row;
-    s_shape = ds->shape;
+    const int64_t st = ds->step;
+    s_row = st >= 0 && st < ds->n && ds->active[st] ? ds->q + st * HS2G_MAX_CLASSES : kZeroRow;
   }
   __syncthreads();
-  const double* qrow = s_row;
-  const int no_table = 0;  // the table comes from qrow
-  if (qrow)
-    sweep_x_body<true, false, kXLines, PITCH, true>(d, T, c, vclass, nullptr, s_shape, no_table, qrow, W0, 0, 0, sr,
-                                                    sa, sq);
-  else
-    sweep_x_body<false, false, kXLines, PITCH, true>(d, T, c, vclass, nullptr, nullptr, no_table, nullptr, W0, 0, 0,
-                                                     sr, sa, sq);
-  if (threadIdx.x == 0) {  // the body ends with a barrier: every thread of the CTA is done with the clock
-    __threadfence();
-    if (atomicAdd(&ds->ctas_done, 1u) == gridDim.x - 1) {
-      ds->row += 1;
-      if (use_schedule) ds->step += 1;
-      ds->ctas_done = 0;
-      __threadfence();
-    }
-  }
+  const int no_table = 0;  // the table comes from the row
+  sweep_x_body<true, false, kXLines, PITCH, true>(d, T, c, vclass, nullptr, ds->shape, no_table, s_row, W0, 0, 0, sr,
+                                                  sa, sq);
 }
 
 // x sweep over all lines (RANGED false) or the lines [line_begin, line_end) of the host-buffer step
@@ -311,16 +292,16 @@ void launch_x(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_
 #undef HS2G_X
 }
 
-void launch_x_sched(const StepArgs& a, const Coeffs& c, DevSchedule* ds, int use_schedule, cudaStream_t s) {
+void launch_x_row(const StepArgs& a, const Coeffs& c, const DevSchedule* ds, cudaStream_t s) {
   const Dims& d = a.d;
   const unsigned gx = (unsigned)((d.nz * d.ny + kXLines - 1) / kXLines);
   const int pitch = c.px == d.nx ? 0 : c.px == d.nx + 1 ? 1 : 2;
   if (pitch == 0)
-    sweep_x_sched_kernel<0><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, use_schedule, a.W0);
+    sweep_x_row_kernel<0><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, a.W0);
   else if (pitch == 1)
-    sweep_x_sched_kernel<1><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, use_schedule, a.W0);
+    sweep_x_row_kernel<1><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, a.W0);
   else
-    sweep_x_sched_kernel<2><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, use_schedule, a.W0);
+    sweep_x_row_kernel<2><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, a.W0);
 }
 
 // y lines: W1 = s2 * dT1 from W0 = sigma * dT0
@@ -445,14 +426,25 @@ __global__ void surface_estimate_kernel(int64_t nxy, const double* __restrict__ 
 }
 
 inline unsigned blocks(int64_t n, int per) { return (unsigned)((n + per - 1) / per); }
-// History of a scheduled step into row ds->row - 1 of hist (the step's x sweep advanced the row): layer `layer`
-// of T, or (dz2 > 0) the surface estimate.
+// History of a step into row ds->row of hist: layer `layer` of T, or (dz2 > 0) the surface estimate; the last
+// CTA to finish advances the row (every CTA read it at its start).
 __global__ void history_row_kernel(int64_t nxy, const double* __restrict__ T, int layer, double dz2,
-                                   double* __restrict__ hist, const DevSchedule* __restrict__ ds) {
+                                   double* __restrict__ hist, DevSchedule* ds) {
+  __shared__ int64_t s_row;
+  if (threadIdx.x == 0) s_row = *(volatile int64_t*)&ds->row;
+  __syncthreads();
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= nxy) return;
-  double* dst = hist + (ds->row - 1) * nxy;
-  dst[t] = dz2 > 0.0 ? surface_value(T[t], T[nxy + t], dz2) : T[(int64_t)layer * nxy + t];
+  if (t < nxy)
+    hist[s_row * nxy + t] = dz2 > 0.0 ? surface_value(T[t], T[nxy + t], dz2) : T[(int64_t)layer * nxy + t];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&ds->hist_done, 1u) == gridDim.x - 1) {
+      ds->row = s_row + 1;
+      ds->hist_done = 0;
+      __threadfence();
+    }
+  }
 }
 
 __global__ void schedule_flags_kernel(const double* __restrict__ q, int64_t nrows, uint8_t* __restrict__ active) {
@@ -546,14 +538,13 @@ cudaError_t launch_step(const StepArgs& a, const Coeffs& c, const QTable& q, cud
   return launch_step_events(a, c, q, s, nullptr);
 }
 
-cudaError_t launch_step_scheduled(const StepArgs& a, const Coeffs& c, DevSchedule* ds, bool use_schedule,
-                                  cudaStream_t s) {
-  launch_x_sched(a, c, ds, use_schedule ? 1 : 0, s);
+cudaError_t launch_step_row(const StepArgs& a, const Coeffs& c, const DevSchedule* ds, cudaStream_t s) {
+  launch_x_row(a, c, ds, s);
   return launch_yz(a, c, s, nullptr);
 }
 
-cudaError_t launch_history_row(const Dims& d, const double* T, int layer, double dz2, double* hist,
-                               const DevSchedule* ds, cudaStream_t s) {
+cudaError_t launch_history_row(const Dims& d, const double* T, int layer, double dz2, double* hist, DevSchedule* ds,
+                               cudaStream_t s) {
   history_row_kernel<<<blocks(d.nxy(), 256), 256, 0, s>>>(d.nxy(), T, layer, dz2, hist, ds);
   return cudaGetLastError();
 }

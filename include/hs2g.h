@@ -168,10 +168,11 @@ int hs2g_step(hs2g_handle* h, const double* T_in, double* T_out, const double* q
 
 /*
  * nsteps timesteps on the device (replaces the reference's run_adi_steps loop over a run's times,
- * alternatingdirection_c_pyx.pyx:387-416).  After the first step (queued directly when T_in != T_out) every
- * step is one replay of a captured CUDA graph of the in-place step, whose x sweep reads the step's class
- * sources from the handle's device schedule at the schedule clock (hs2g_set_schedule) and whose last kernel
- * advances the clock; graphs are kept per (T buffer, history buffer, layer) and reused by later calls.
+ * alternatingdirection_c_pyx.pyx:387-416).  After the first step (queued directly when T_in != T_out) the steps
+ * are replays of captured CUDA graphs of the in-place step: a step whose schedule row has a source replays a
+ * one-step graph whose x sweep reads that row of the handle's device schedule (hs2g_set_schedule) on the
+ * device, and runs of steps without one replay a graph of four steps (or one); graphs are kept per (T buffer,
+ * history buffer, layer) and reused by later calls.
  *   qtabs  host array [nsteps][HS2G_MAX_CLASSES] of per-step class sources: replaces the handle's schedule
  *          (as hs2g_set_schedule with these rows, clock 0) before the steps; or NULL: with HS2G_SCHEDULED the
  *          steps take rows from the schedule already set, from its clock on (rows past its end: no source),
@@ -222,13 +223,16 @@ int hs2g_source_table(int nsrc, const int32_t* kind, const double* params, doubl
 /*
  * Device-resident source schedule of a handle (the batched form's hs2g_batch_set_sources for one problem):
  * qtabs[nsteps][HS2G_MAX_CLASSES] class source values (W/m^3) for steps 0 .. nsteps-1, a host array or, with
- * HS2G_DEVICE, a device array copied on the handle's stream.  Sets the clock to 0; a step reads row `clock`
- * (none when clock >= nsteps; nsteps = 0 clears the schedule) and advances the clock.  Row values multiply the
- * per-voxel source shapes as hs2g_step's qtab does (hs2g_source_zdecay / hs2g_source_point, as they stand when
- * the run is queued).  Steps queued earlier on the handle's stream read the rows they were queued with.
+ * HS2G_DEVICE, a device array, copied on the handle's stream; the call then waits for the stream to read back
+ * one flag per row (any non-zero value), from which hs2g_run picks each step's graph.  Sets the clock to 0; a
+ * scheduled step takes row `clock` (none when clock >= nsteps; nsteps = 0 clears the schedule) and advances the
+ * clock.  Row values multiply the per-voxel source shapes as hs2g_step's qtab does (hs2g_source_zdecay /
+ * hs2g_source_point, as they stand when the run is queued).  Steps queued earlier read the rows they were
+ * queued with.
  */
 int hs2g_set_schedule(hs2g_handle* h, int64_t nsteps, const double* qtabs, int flags);
-/* Set the schedule clock (queued on the handle's stream), or read it (waits for the stream). */
+/* Set or read the schedule clock: the row of the next scheduled step, counted by the steps queued (no device
+   work). */
 int hs2g_set_clock(hs2g_handle* h, int64_t step);
 int hs2g_get_clock(hs2g_handle* h, int64_t* step);
 
