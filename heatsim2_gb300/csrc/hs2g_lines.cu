@@ -167,6 +167,12 @@ __global__ void __launch_bounds__(kNL) line_sweep_tma_kernel(Geometry g, const _
   auto tile = [&](int s, int arr) { return tiles + ((int64_t)s * NA + arr) * (kNL * kRows); };
 
   if (tid == 0) {
+    // fetch the tensor-map descriptors while the barriers are set up (the first copies would wait for them)
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&mA) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&mAlpha) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&mScratch) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&mBeta) : "memory");
+    if (ADD_T) asm volatile("prefetch.tensormap [%0];" ::"l"(&mT) : "memory");
     for (int s = 0; s < kSlots; ++s) mbar_init(&bars[s], 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");

@@ -19,6 +19,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 #include "hs2g_internal.cuh"
 
@@ -205,11 +206,15 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
 // instance without a source also gets 72 registers and takes 334 us, while the instances with a source term or
 // padded W0 rows take 78-80 registers there, 6 CTAs per SM, two waves: 694 us for a source step).  Padded rows
 // of an odd nx use the one-column index (349 us at 65x512x511; with a general pitch 362 us).
+// The class table is a kernel parameter only in the instances with a source (2 KB that the others would copy at
+// every launch for nothing).
+template <bool HAS_Q>
+using XTable = typename std::conditional<HAS_Q, QTable, int>::type;
 template <bool HAS_Q, bool RANGED, int LINES, int PITCH>
 __global__ void __maxnreg__(72) sweep_x_lean_kernel(Dims d, const double* __restrict__ T, Coeffs c,
                                                     const uint8_t* __restrict__ vclass,
                                                     const double* __restrict__ qdense,
-                                                    const double* __restrict__ qshape, QTable qt,
+                                                    const double* __restrict__ qshape, XTable<HAS_Q> qt,
                                                     double* __restrict__ W0, int64_t line_begin, int64_t line_end) {
   __shared__ double sr[LINES][kXChunk + 1];
   __shared__ double sa[LINES][kXChunk + 1];
@@ -223,7 +228,7 @@ template <bool HAS_Q, bool RANGED, int LINES = kXLines>
 __global__ void __launch_bounds__(kXThreads, kXMinBlocks) sweep_x_kernel(Dims d, const double* __restrict__ T, Coeffs c,
                                                              const uint8_t* __restrict__ vclass,
                                                              const double* __restrict__ qdense,
-                                                             const double* __restrict__ qshape, QTable qt,
+                                                             const double* __restrict__ qshape, XTable<HAS_Q> qt,
                                                              double* __restrict__ W0, int64_t line_begin,
                                                              int64_t line_end) {
   __shared__ double sr[LINES][kXChunk + 1];
@@ -265,29 +270,29 @@ void launch_x(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_
   const unsigned gx = (unsigned)(((RANGED ? line_end - line_begin : d.nz * d.ny) + LINES - 1) / LINES);
   const bool has_q = a.has_qtab || a.qdense != nullptr;
   const int pitch = c.px == d.nx ? 0 : c.px == d.nx + 1 ? 1 : 2;
-#define HS2G_X(KERNEL, ...) \
-  KERNEL<__VA_ARGS__><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, a.qshape, q, a.W0, line_begin, \
+#define HS2G_X(KERNEL, TABLE, ...) \
+  KERNEL<__VA_ARGS__><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, a.qshape, TABLE, a.W0, line_begin, \
                                                line_end)
   if (RANGED && pitch == 0) {
     if (has_q)
-      HS2G_X(sweep_x_kernel, true, RANGED, LINES);
+      HS2G_X(sweep_x_kernel, q, true, RANGED, LINES);
     else
-      HS2G_X(sweep_x_kernel, false, RANGED, LINES);
+      HS2G_X(sweep_x_kernel, 0, false, RANGED, LINES);
   } else if (pitch == 0) {
     if (has_q)
-      HS2G_X(sweep_x_lean_kernel, true, RANGED, LINES, 0);
+      HS2G_X(sweep_x_lean_kernel, q, true, RANGED, LINES, 0);
     else
-      HS2G_X(sweep_x_lean_kernel, false, RANGED, LINES, 0);
+      HS2G_X(sweep_x_lean_kernel, 0, false, RANGED, LINES, 0);
   } else if (pitch == 1) {
     if (has_q)
-      HS2G_X(sweep_x_lean_kernel, true, RANGED, LINES, 1);
+      HS2G_X(sweep_x_lean_kernel, q, true, RANGED, LINES, 1);
     else
-      HS2G_X(sweep_x_lean_kernel, false, RANGED, LINES, 1);
+      HS2G_X(sweep_x_lean_kernel, 0, false, RANGED, LINES, 1);
   } else {
     if (has_q)
-      HS2G_X(sweep_x_lean_kernel, true, RANGED, LINES, 2);
+      HS2G_X(sweep_x_lean_kernel, q, true, RANGED, LINES, 2);
     else
-      HS2G_X(sweep_x_lean_kernel, false, RANGED, LINES, 2);
+      HS2G_X(sweep_x_lean_kernel, 0, false, RANGED, LINES, 2);
   }
 #undef HS2G_X
 }

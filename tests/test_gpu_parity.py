@@ -132,6 +132,20 @@ def _compare_with_oracle(spec, nsteps, tol=TOL):
     return T
 
 
+def test_fixed_planes_at_both_ends_vs_oracle(cuda_ok):
+    """Planes of fixed voxels at the top (the ambient layer) and at the bottom: host-buffer steps match the
+    oracle, and a run in place on the device matches the single steps."""
+    spec = W.composite_panel(seed=8, nz=20, ny=40, nx=48, top_layers=6, width_range=(4, 12), depth_range=(2, 12),
+                             nsteps=6)
+    spec["arrays"]["material"][-2:] = 2             # two fixed planes at the bottom
+    T = _compare_with_oracle(spec, 6)
+    import torch
+    P, S = _setup(spec)
+    got = hs.run(P, torch.from_numpy(W.initial_temperature(spec)).cuda(), W.step_times(spec, 6), spec["dt"],
+                 spec["arrays"]["volumetric"], W.volumetric_tuple(hs, spec))
+    np.testing.assert_array_equal(got.cpu().numpy(), T)
+
+
 def test_composite_panel_midsize_vs_oracle(cuda_ok):
     spec = W.composite_panel(seed=3, nz=40, ny=96, nx=80, top_layers=10, width_range=(8, 30),
                              depth_range=(3, 30))
