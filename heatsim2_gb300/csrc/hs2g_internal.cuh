@@ -58,6 +58,29 @@ struct DevSchedule {
   unsigned int hist_done;  // CTAs of the current history kernel that have finished (the last one advances row)
 };
 
+// L2 eviction policies (createpolicy) and stores that carry one: evict-first for data streamed once, evict-last
+// for a value the same thread block reads back soon (a sweep's forward values), and dropping a 128-byte line
+// without writing it back (its contents are undefined until written again).
+__device__ __forceinline__ uint64_t l2_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ void st_hint(double* p, double v, uint64_t policy) {
+  asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(v), "l"(policy) : "memory");
+}
+__device__ __forceinline__ void st_hint(float* p, float v, uint64_t policy) {
+  asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(policy) : "memory");
+}
+__device__ __forceinline__ void l2_discard_line(const void* p) {
+  asm volatile("discard.global.L2 [%0], 128;" ::"l"(p) : "memory");
+}
+
 // Record the message hs2g_last_error() returns for this thread (hs2g_api.cu); returns code.
 int set_last_error(int code, const char* message);
 

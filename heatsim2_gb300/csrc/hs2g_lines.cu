@@ -104,21 +104,11 @@ __device__ __forceinline__ void tile_load(void* dst, const CUtensorMap* map, int
         "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(saddr(bar))
         : "memory");
 }
-__device__ __forceinline__ uint64_t policy_evict_first() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ uint64_t policy_evict_last() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
 // store of a value the same kernel reads back soon (the forward sweep's scratch): kept in L2 with HINT
 template <bool HINT>
 __device__ __forceinline__ void st_keep(double* p, double v, uint64_t policy) {
   if (HINT)
-    asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(v), "l"(policy) : "memory");
+    st_hint(p, v, policy);
   else
     *p = v;
 }
@@ -181,8 +171,8 @@ __global__ void __launch_bounds__(kNL) line_sweep_tma_kernel(Geometry g, const _
 
   SlotRing ring;  // slot phases; pending slots are tracked by the producer (tid 0), which issues every copy
   const int cx = (int)i0, cz = (int)plane;
-  const uint64_t pol_first = HINT ? policy_evict_first() : 0;
-  const uint64_t pol_last = HINT ? policy_evict_last() : 0;
+  const uint64_t pol_first = HINT ? l2_evict_first() : 0;
+  const uint64_t pol_last = HINT ? l2_evict_last() : 0;
 
   auto issue_fwd = [&](int64_t q) {  // tile q covers rows [q*kRows, q*kRows + kRows)
     const int s = (int)(q % kSlots);

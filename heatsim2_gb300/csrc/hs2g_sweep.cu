@@ -46,14 +46,6 @@ constexpr int kLineThreads = 128;
 // A sweep's forward values are written and read back by the same thread block within microseconds; with
 // every line in flight they add up to more than L2 (136 MB at 65x512x512), so they are stored with an
 // evict-last L2 policy where that keeps them on chip.
-__device__ __forceinline__ uint64_t l2_policy_last() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ void st_keep(double* p, double v, uint64_t policy) {
-  asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(v), "l"(policy) : "memory");
-}
 template <bool HAS_Q>
 __device__ __forceinline__ double stencil_x(const Dims& d, const double* __restrict__ T, const Coeffs& c,
                                             const uint8_t* __restrict__ vclass, const double* __restrict__ qdense,
@@ -333,11 +325,6 @@ __global__ void __launch_bounds__(kLineThreads) sweep_y_kernel(Dims d, const dou
   }
 }
 
-// Drop a 128-byte L2 line without writing it back: its contents become undefined until written again.
-__device__ __forceinline__ void discard_line(const double* p) {
-  asm volatile("discard.global.L2 [%0], 128;" ::"l"(p) : "memory");
-}
-
 // z lines: dT2 from W1 = s2 * dT1; T_out = T_in + dT2.  Z is scratch (the x sweep's buffer, free by now).
 // T_in may equal T_out: each voxel's T_in is read by the same thread just before its T_out is written.
 // DISCARD: the forward values are read once by the back substitution and never again, so once a warp has read
@@ -362,12 +349,12 @@ __global__ void __launch_bounds__(kLineThreads, 16) sweep_z_kernel(Dims d, const
   const int64_t jw = t / d.nx;
   int64_t pw = jw * px + (t - jw * d.nx);
   const int64_t nxyw = d.ny * px;
-  const uint64_t keep = l2_policy_last();  // the forward values come back to this thread after its last row
+  const uint64_t keep = l2_evict_last();  // the forward values come back to this thread after its last row
   double z = 0.0;
 #pragma unroll 4
   for (int64_t k = 0; k < d.nz; ++k, p += nxy, pw += nxyw) {
     z = fma(-a2[p], z, W1[pw]);
-    st_keep(Z + p, z, keep);
+    st_hint(Z + p, z, keep);
   }
   double x = 0.0;
   if (!DISCARD) {
@@ -401,10 +388,10 @@ __global__ void __launch_bounds__(kLineThreads, 16) sweep_z_kernel(Dims d, const
     if (!drop) continue;
     __syncwarp();  // every lane of the warp has read its four rows of Z
     if ((threadIdx.x & 15) == 0) {
-      discard_line(Z + p);
-      discard_line(Z + p + nxy);
-      discard_line(Z + p + 2 * nxy);
-      discard_line(Z + p + 3 * nxy);
+      l2_discard_line(Z + p);
+      l2_discard_line(Z + p + nxy);
+      l2_discard_line(Z + p + 2 * nxy);
+      l2_discard_line(Z + p + 3 * nxy);
     }
   }
 }
