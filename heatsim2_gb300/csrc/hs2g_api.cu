@@ -844,8 +844,8 @@ int write_schedule_header(hs2g_handle* h) {
 
 // Replace the schedule's rows by qtabs[nsteps][HS2G_MAX_CLASSES] (host, or device when device_ptr) and set the
 // clock to 0.  Work already queued on the handle's stream reads the old rows before they are overwritten.  The
-// flags (row has a non-zero value) are computed on the device and mirrored on the host, which picks each step's
-// graph from them.
+// flags (row has a non-zero value) are kept on both sides: the host picks each step's graph from them.  Host
+// rows are flagged on the host; device rows on the device, and read back (the call then waits for the stream).
 int set_schedule_rows(hs2g_handle* h, int64_t nsteps, const double* qtabs, bool device_ptr) {
   int rc = ensure_schedule(h);
   if (rc) return rc;
@@ -863,11 +863,21 @@ int set_schedule_rows(hs2g_handle* h, int64_t nsteps, const double* qtabs, bool 
     HS2G_CUDA(cudaMemcpyAsync(h->sched_q, qtabs, sizeof(double) * HS2G_MAX_CLASSES * (size_t)nsteps,
                               device_ptr ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream),
               "upload source schedule");
-    HS2G_CUDA(hs2g::launch_schedule_flags(h->sched_q, nsteps, h->sched_active, h->stream), "schedule flags");
-    HS2G_CUDA(cudaMemcpyAsync(h->sched_flags.data(), h->sched_active, (size_t)nsteps, cudaMemcpyDeviceToHost,
-                              h->stream),
-              "read schedule flags");
-    HS2G_CUDA(cudaStreamSynchronize(h->stream), "source schedule");
+    if (device_ptr) {
+      HS2G_CUDA(hs2g::launch_schedule_flags(h->sched_q, nsteps, h->sched_active, h->stream), "schedule flags");
+      HS2G_CUDA(cudaMemcpyAsync(h->sched_flags.data(), h->sched_active, (size_t)nsteps, cudaMemcpyDeviceToHost,
+                                h->stream),
+                "read schedule flags");
+      HS2G_CUDA(cudaStreamSynchronize(h->stream), "source schedule");
+    } else {
+      for (int64_t r = 0; r < nsteps; ++r)
+        for (int c = 0; c < HS2G_MAX_CLASSES && !h->sched_flags[(size_t)r]; ++c)
+          h->sched_flags[(size_t)r] = qtabs[r * HS2G_MAX_CLASSES + c] != 0.0;
+      // pageable source: staged before the call returns, so the flags may change on the host afterwards
+      HS2G_CUDA(cudaMemcpyAsync(h->sched_active, h->sched_flags.data(), (size_t)nsteps, cudaMemcpyHostToDevice,
+                                h->stream),
+                "upload schedule flags");
+    }
   }
   h->sched_n = nsteps;
   h->clock = 0;

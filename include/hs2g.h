@@ -223,8 +223,9 @@ int hs2g_source_table(int nsrc, const int32_t* kind, const double* params, doubl
 /*
  * Device-resident source schedule of a handle (the batched form's hs2g_batch_set_sources for one problem):
  * qtabs[nsteps][HS2G_MAX_CLASSES] class source values (W/m^3) for steps 0 .. nsteps-1, a host array or, with
- * HS2G_DEVICE, a device array, copied on the handle's stream; the call then waits for the stream to read back
- * one flag per row (any non-zero value), from which hs2g_run picks each step's graph.  Sets the clock to 0; a
+ * HS2G_DEVICE, a device array, copied on the handle's stream.  One flag per row (any non-zero value) is kept on
+ * the host, from which hs2g_run picks each step's graph: for device rows the call computes them on the device
+ * and waits for the stream to read them back.  Sets the clock to 0; a
  * scheduled step takes row `clock` (none when clock >= nsteps; nsteps = 0 clears the schedule) and advances the
  * clock.  Row values multiply the per-voxel source shapes as hs2g_step's qtab does (hs2g_source_zdecay /
  * hs2g_source_point, as they stand when the run is queued).  Steps queued earlier read the rows they were

@@ -179,3 +179,19 @@ def test_run_with_shaped_sources_equals_single_steps(cuda_ok, shape):
     for s in range(len(times)):
         np.testing.assert_array_equal(hist[s], steps[s][1])
     assert np.abs(steps[2] - steps[1]).max() > 1e-3 and np.abs(steps[4] - steps[3]).max() > 1e-6
+
+
+def test_schedule_arguments(cuda_ok):
+    """Bad schedule arguments are refused before anything is queued, and the handle keeps working."""
+    spec, P, qtabs = _problem(shape=(8, 32, 32), nsteps=4)
+    L = _native.load()
+    h = P.handle.ptr
+    assert L.hs2g_set_schedule(h, -1, qtabs.ctypes.data, 0) == _native.ERR_ARG
+    assert L.hs2g_set_schedule(h, 3, None, 0) == _native.ERR_ARG
+    assert L.hs2g_set_clock(h, -2) == _native.ERR_ARG
+    assert L.hs2g_get_clock(h, None) == _native.ERR_ARG
+    _native.check(L.hs2g_set_schedule(h, len(qtabs), qtabs.ctypes.data, 0))
+    T0 = torch.from_numpy(W.initial_temperature(spec)).cuda()
+    T = T0.clone()
+    _scheduled(P, T, 4)
+    assert torch.equal(T, _host_launched(P, T0, qtabs))
