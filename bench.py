@@ -195,8 +195,9 @@ def _cpu_impl():
     return "port", (oracle, HS)
 
 
-def cpu_worker(kind_req, seconds, max_steps, barrier=None, result=None):
-    """Time one CPU implementation on the composite panel at CPU_SAMPLE_SHAPE; returns a dict."""
+def cpu_worker(kind_req, seconds, max_steps, barrier=None, result=None, warm=1):
+    """Time one CPU implementation on the composite panel at CPU_SAMPLE_SHAPE after `warm` untimed steps;
+    returns a dict."""
     import contextlib
     import io
     from heatsim2_gb300 import workloads as W
@@ -215,12 +216,13 @@ def cpu_worker(kind_req, seconds, max_steps, barrier=None, result=None):
         step = lambda t, T: orc.run_adi_steps(P, None, t, spec["dt"], T, spec["arrays"]["volumetric"], vol)
     T = W.initial_temperature(spec)
     times = W.step_times(spec, max_steps)
-    T = step(times[0], T)          # warm-up (first step)
+    for t in times[:warm]:         # warm-up
+        T = step(t, T)
     if barrier is not None:
         barrier.wait()
     t0 = time.perf_counter()
     n = 0
-    for t in times[1:]:
+    for t in times[warm:]:
         T = step(t, T)
         n += 1
         if seconds and time.perf_counter() - t0 >= seconds:
@@ -271,7 +273,9 @@ def reference_arm(args, world, rank):
     barrier = ctx.Barrier(nproc)
     q = ctx.Queue()
     steps = max(1, args.steps)
-    procs = [ctx.Process(target=cpu_worker, args=("auto", 0.0, steps + 1, barrier, q)) for _ in range(nproc)]
+    warm = max(1, args.warmup)
+    procs = [ctx.Process(target=cpu_worker, args=("auto", 0.0, steps + warm, barrier, q, warm))
+             for _ in range(nproc)]
     for p in procs:
         p.start()
     res = [q.get() for _ in procs]
@@ -283,7 +287,7 @@ def reference_arm(args, world, rank):
     nz, ny, nx = CPU_SAMPLE_SHAPE
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
-        "steps": steps, "warmup": 1, "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "composite panel %dx%dx%d (+ambient), one independent instance per host core"
                                % (nz, ny, nx), "processes": nproc},
