@@ -65,6 +65,7 @@ struct hs2g_handle {
   unsigned long long* err_dev = nullptr;
   int* status_dev = nullptr;
   bool bulk_y = false, bulk_z = false, z_discard = true;
+  bool graph_pdl = true;  // the captured step graphs launch their sweeps with programmatic dependent launch
   bool per_row = false;  // compiled from per-row conductances (hs2g_create_rows): no shared face arrays
   hs2g::TensorMapCache* tmaps = nullptr;
   int64_t bytes = 0;
@@ -241,11 +242,15 @@ int alloc_common(hs2g_handle* h, bool faces = true) {
   HS2G_CUDA(hs2g::lines_bulk_prepare(), "configure line-sweep kernels");
   // Kernel variants (defaults are the fastest measured on GB300; the others stay selectable for comparison
   // and testing): HS2G_LINE_SWEEP=plain the plain-load y sweep, HS2G_Z_SWEEP=tma the TMA tensor-tile z sweep,
-  // HS2G_Z_DISCARD=0 the plain z sweep leaving its forward values to L2's own eviction.
+  // HS2G_Z_DISCARD=0 the plain z sweep leaving its forward values to L2's own eviction, HS2G_PDL=0 the step
+  // graphs' sweeps launched without programmatic dependent launch (0.5702 against 0.5689 ms per step at
+  // 65x512x512).
   const char* ymode = getenv("HS2G_LINE_SWEEP");
   const char* zmode = getenv("HS2G_Z_SWEEP");
   const char* zdiscard = getenv("HS2G_Z_DISCARD");
+  const char* pdl = getenv("HS2G_PDL");
   h->z_discard = !(zdiscard && strcmp(zdiscard, "0") == 0);
+  h->graph_pdl = !(pdl && strcmp(pdl, "0") == 0);
   h->bulk_y = !(ymode && strcmp(ymode, "plain") == 0) && hs2g::lines_bulk_supported(h->d, 1, h->c.px);
   h->bulk_z = (zmode && strcmp(zmode, "tma") == 0) && h->c.px == h->d.nx && (n % 2 == 0) &&
               hs2g::lines_bulk_supported(h->d, 2, h->d.nx);
@@ -887,10 +892,12 @@ int set_schedule_rows(hs2g_handle* h, int64_t nsteps, const double* qtabs, bool 
 // One step src -> dst queued on s: with `source`, the x sweep whose class table is the schedule's row at the
 // device clock (set by the caller), else the x sweep without a source; then y, z and the history row.
 cudaError_t queue_step(hs2g_handle* h, const double* src, double* dst, double* hist, int layer, double dz2,
-                       bool source, cudaStream_t s) {
+                       bool source, cudaStream_t s, bool pdl = false, bool pdl_x = false) {
   hs2g::StepArgs a = make_args(h, src, dst);
   a.T_in = src;
   a.T_out = dst;
+  a.pdl = pdl;
+  a.pdl_x = pdl_x;
   cudaError_t e;
   if (source) {
     e = hs2g::launch_step_row(a, h->c, h->sched_dev, s);
@@ -900,7 +907,7 @@ cudaError_t queue_step(hs2g_handle* h, const double* src, double* dst, double* h
     a.has_qtab = false;
     e = hs2g::launch_step(a, h->c, q, s);
   }
-  if (e == cudaSuccess && hist) e = hs2g::launch_history_row(h->d, dst, layer, dz2, hist, h->sched_dev, s);
+  if (e == cudaSuccess && hist) e = hs2g::launch_history_row(h->d, dst, layer, dz2, hist, h->sched_dev, s, pdl);
   return e;
 }
 
@@ -919,7 +926,7 @@ int step_graph(hs2g_handle* h, double* T, double* hist, int layer, double dz2, b
   HS2G_CUDA(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal), "begin step capture");
   cudaError_t e = cudaSuccess;
   for (int k = 0; k < steps && e == cudaSuccess; ++k)
-    e = queue_step(h, T, T, hist, layer, dz2, source, h->cap_stream);
+    e = queue_step(h, T, T, hist, layer, dz2, source, h->cap_stream, h->graph_pdl, h->graph_pdl && k > 0);
   cudaGraph_t g = nullptr;
   const cudaError_t e_end = cudaStreamEndCapture(h->cap_stream, &g);
   if (e == cudaSuccess) e = e_end;

@@ -81,6 +81,31 @@ __device__ __forceinline__ void l2_discard_line(const void* p) {
   asm volatile("discard.global.L2 [%0], 128;" ::"l"(p) : "memory");
 }
 
+// Programmatic dependent launch inside the captured step graphs: a sweep launched with the attribute may be set
+// up on the SMs while the sweep before it on the stream completes (no kernel triggers early, so that happens
+// only once every CTA of the previous sweep has exited, and the CTAs of the new one spread over the whole GPU as
+// in an ordinary launch).  Each sweep waits here, before it touches memory the previous one reads or writes,
+// until that sweep has completed and its writes are visible.  A no-op in a kernel launched without the
+// attribute.
+__device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Kernel launch with the programmatic-serialization attribute when pdl is set (an ordinary launch otherwise).
+template <typename... P, typename... A>
+cudaError_t launch_kernel(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool pdl,
+                          A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<A&&>(args)...);
+}
+
 // Record the message hs2g_last_error() returns for this thread (hs2g_api.cu); returns code.
 int set_last_error(int code, const char* message);
 
@@ -133,6 +158,8 @@ struct StepArgs {
   bool bulk_y, bulk_z;   // use the TMA tensor-tile line sweeps (hs2g_lines.cu) for y / z
   bool z_discard;        // the plain z sweep drops its forward values from L2 after reading them
   struct TensorMapCache* tmaps;
+  bool pdl;              // launch the y and z sweeps with programmatic dependent launch (captured step graphs)
+  bool pdl_x;            // the same for the x sweep (not for the first kernel of a graph)
 };
 
 // TMA tensor-tile line sweeps (hs2g_lines.cu); axis 1 = y, 2 = z.
@@ -144,7 +171,7 @@ cudaError_t lines_bulk_prepare();
 // axis 1 (y): A, alpha, scratch, beta and out have row pitch px; axis 2 (z): every array has pitch nx (px = nx)
 cudaError_t launch_lines_bulk(const Dims& d, int axis, const double* A, const double* alpha, double* scratch,
                               const double* beta, const double* T_in, double* out, int* status,
-                              TensorMapCache* cache, cudaStream_t s, int64_t px);
+                              TensorMapCache* cache, cudaStream_t s, int64_t px, bool pdl = false);
 cudaError_t launch_step(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s);
 // the same three kernels with an event recorded before each and after the last (ev[0..3])
 cudaError_t launch_step_events(const StepArgs& a, const Coeffs& c, const QTable& q, cudaStream_t s,
@@ -157,7 +184,7 @@ cudaError_t launch_step_row(const StepArgs& a, const Coeffs& c, const DevSchedul
 // z = 0 surface estimate from layers 0 and 1 with dz2 = dz**2 (dz2 > 0); the kernel's last CTA advances
 // ds->row.
 cudaError_t launch_history_row(const Dims& d, const double* T, int layer, double dz2, double* hist, DevSchedule* ds,
-                               cudaStream_t s);
+                               cudaStream_t s, bool pdl = false);
 // the reference's dz**2.0 (the C library's pow)
 double surface_dz2(double dz);
 // one flag per schedule row: active[s] = any of q[s][0..nclass-1] non-zero

@@ -167,6 +167,7 @@ __global__ void __launch_bounds__(kNL) line_sweep_tma_kernel(Geometry g, const _
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  wait_prior_grid();  // the inputs come from the previous sweep; the outputs overwrite what it read
   __syncthreads();
 
   SlotRing ring;  // slot phases; pending slots are tracked by the producer (tid 0), which issues every copy
@@ -347,7 +348,7 @@ cudaError_t lines_bulk_prepare() {
 
 cudaError_t launch_lines_bulk(const Dims& d, int axis, const double* A, const double* alpha, double* scratch,
                               const double* beta, const double* T_in, double* out, int* status,
-                              TensorMapCache* cache, cudaStream_t s, int64_t px) {
+                              TensorMapCache* cache, cudaStream_t s, int64_t px, bool pdl) {
   if (!aligned16(A) || !aligned16(alpha) || !aligned16(scratch) || !aligned16(beta) || !aligned16(out) ||
       (T_in && !aligned16(T_in)) || !cache)
     return cudaErrorMisalignedAddress;
@@ -366,21 +367,19 @@ cudaError_t launch_lines_bulk(const Dims& d, int axis, const double* A, const do
     g.nrows = d.ny;
     const char* slots = getenv("HS2G_Y_SLOTS");
     if (slots && strcmp(slots, "3") == 0)
-      line_sweep_tma_kernel<false, true, 3><<<(unsigned)(d.nz * g.groups), kNL, smem_bytes<false, 3>(), s>>>(
-          g, mA, mAl, mS, mB, mT, scratch, out, status);
-    else
-      line_sweep_tma_kernel<false, true><<<(unsigned)(d.nz * g.groups), kNL, smem_bytes<false>(), s>>>(
-          g, mA, mAl, mS, mB, mT, scratch, out, status);
+      return launch_kernel(line_sweep_tma_kernel<false, true, 3>, dim3((unsigned)(d.nz * g.groups)), dim3(kNL),
+                           smem_bytes<false, 3>(), s, pdl, g, mA, mAl, mS, mB, mT, scratch, out, status);
+    return launch_kernel(line_sweep_tma_kernel<false, true>, dim3((unsigned)(d.nz * g.groups)), dim3(kNL),
+                         smem_bytes<false>(), s, pdl, g, mA, mAl, mS, mB, mT, scratch, out, status);
   } else {
     g.groups = (d.nxy() + kNL - 1) / kNL;
     g.plane_stride = 0;
     g.width = d.nxy();
     g.stride = d.nxy();
     g.nrows = d.nz;
-    line_sweep_tma_kernel<true><<<(unsigned)g.groups, kNL, smem_bytes<true>(), s>>>(g, mA, mAl, mS, mB, mT,
-                                                                                    scratch, out, status);
+    return launch_kernel(line_sweep_tma_kernel<true>, dim3((unsigned)g.groups), dim3(kNL), smem_bytes<true>(), s, pdl,
+                         g, mA, mAl, mS, mB, mT, scratch, out, status);
   }
-  return cudaGetLastError();
 }
 
 

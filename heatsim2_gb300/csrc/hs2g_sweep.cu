@@ -115,6 +115,7 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
   const int64_t nlines = RANGED ? line_end : d.nz * d.ny;
   const int64_t L0 = (RANGED ? line_begin : 0) + (int64_t)blockIdx.x * LINES;
   const int nchunks = (int)((d.nx + kXChunk - 1) / kXChunk);
+  wait_prior_grid();  // T comes from the previous step's z sweep, which used W0 as its scratch
   __syncthreads();
 
   // forward: z_i = R'_i - a0_i * z_{i-1}
@@ -262,9 +263,9 @@ void launch_x(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_
   const unsigned gx = (unsigned)(((RANGED ? line_end - line_begin : d.nz * d.ny) + LINES - 1) / LINES);
   const bool has_q = a.has_qtab || a.qdense != nullptr;
   const int pitch = c.px == d.nx ? 0 : c.px == d.nx + 1 ? 1 : 2;
-#define HS2G_X(KERNEL, TABLE, ...) \
-  KERNEL<__VA_ARGS__><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, a.qdense, a.qshape, TABLE, a.W0, line_begin, \
-                                               line_end)
+#define HS2G_X(KERNEL, TABLE, ...)                                                                             \
+  launch_kernel(KERNEL<__VA_ARGS__>, dim3(gx), dim3(kXThreads), 0, s, a.pdl_x, d, a.T_in, c, a.vclass, a.qdense, \
+                a.qshape, TABLE, a.W0, line_begin, line_end)
   if (RANGED && pitch == 0) {
     if (has_q)
       HS2G_X(sweep_x_kernel, q, true, RANGED, LINES);
@@ -294,11 +295,11 @@ void launch_x_row(const StepArgs& a, const Coeffs& c, const DevSchedule* ds, cud
   const unsigned gx = (unsigned)((d.nz * d.ny + kXLines - 1) / kXLines);
   const int pitch = c.px == d.nx ? 0 : c.px == d.nx + 1 ? 1 : 2;
   if (pitch == 0)
-    sweep_x_row_kernel<0><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, a.W0);
+    launch_kernel(sweep_x_row_kernel<0>, dim3(gx), dim3(kXThreads), 0, s, a.pdl_x, d, a.T_in, c, a.vclass, ds, a.W0);
   else if (pitch == 1)
-    sweep_x_row_kernel<1><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, a.W0);
+    launch_kernel(sweep_x_row_kernel<1>, dim3(gx), dim3(kXThreads), 0, s, a.pdl_x, d, a.T_in, c, a.vclass, ds, a.W0);
   else
-    sweep_x_row_kernel<2><<<gx, kXThreads, 0, s>>>(d, a.T_in, c, a.vclass, ds, a.W0);
+    launch_kernel(sweep_x_row_kernel<2>, dim3(gx), dim3(kXThreads), 0, s, a.pdl_x, d, a.T_in, c, a.vclass, ds, a.W0);
 }
 
 // y lines: W1 = s2 * dT1 from W0 = sigma * dT0
@@ -306,6 +307,7 @@ __global__ void __launch_bounds__(kLineThreads) sweep_y_kernel(Dims d, const dou
                                                                 const double* __restrict__ a1,
                                                                 const double* __restrict__ b1,
                                                                 double* __restrict__ W1, int64_t px) {
+  wait_prior_grid();
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= d.nz * d.nx) return;
   const int64_t k = t / d.nx, i = t - k * d.nx;
@@ -344,6 +346,7 @@ __global__ void __launch_bounds__(kLineThreads, 16) sweep_z_kernel(Dims d, const
   const int64_t nxy = d.nxy();
   const int64_t t0 = t - (threadIdx.x & 31);  // the warp's first column
   const bool drop = DISCARD && nxy % 16 == 0 && t0 % 32 == 0 && t0 + 32 <= col_end;  // warp-uniform
+  wait_prior_grid();
   if (t >= col_end) return;
   int64_t p = t;
   const int64_t jw = t / d.nx;
@@ -423,6 +426,7 @@ inline unsigned blocks(int64_t n, int per) { return (unsigned)((n + per - 1) / p
 __global__ void history_row_kernel(int64_t nxy, const double* __restrict__ T, int layer, double dz2,
                                    double* __restrict__ hist, DevSchedule* ds) {
   __shared__ int64_t s_row;
+  wait_prior_grid();
   if (threadIdx.x == 0) s_row = *(volatile int64_t*)&ds->row;
   __syncthreads();
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -503,13 +507,14 @@ cudaError_t launch_yz(const StepArgs& a, const Coeffs& c, cudaStream_t s, cudaEv
   const Dims& d = a.d;
   cudaError_t e = cudaSuccess;
   if (a.bulk_y)
-    e = launch_lines_bulk(d, 1, a.W0, c.a1, a.W1, c.b1, nullptr, a.W1, a.status, a.tmaps, s, c.px);
+    e = launch_lines_bulk(d, 1, a.W0, c.a1, a.W1, c.b1, nullptr, a.W1, a.status, a.tmaps, s, c.px, a.pdl);
   else
-    sweep_y_kernel<<<blocks(d.nz * d.nx, kLineThreads), kLineThreads, 0, s>>>(d, a.W0, c.a1, c.b1, a.W1, c.px);
+    e = launch_kernel(sweep_y_kernel, dim3(blocks(d.nz * d.nx, kLineThreads)), dim3(kLineThreads), 0, s, a.pdl, d,
+                      a.W0, c.a1, c.b1, a.W1, c.px);
   if (e != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[2], s);
   if (a.bulk_z)
-    e = launch_lines_bulk(d, 2, a.W1, c.a2, a.W0, c.b2, a.T_in, a.T_out, a.status, a.tmaps, s, d.nx);
+    e = launch_lines_bulk(d, 2, a.W1, c.a2, a.W0, c.b2, a.T_in, a.T_out, a.status, a.tmaps, s, d.nx, a.pdl);
   else
     e = launch_z_range(a, c, 0, d.nxy(), s);
   if (e != cudaSuccess) return e;
@@ -536,9 +541,9 @@ cudaError_t launch_step_row(const StepArgs& a, const Coeffs& c, const DevSchedul
 }
 
 cudaError_t launch_history_row(const Dims& d, const double* T, int layer, double dz2, double* hist, DevSchedule* ds,
-                               cudaStream_t s) {
-  history_row_kernel<<<blocks(d.nxy(), 256), 256, 0, s>>>(d.nxy(), T, layer, dz2, hist, ds);
-  return cudaGetLastError();
+                               cudaStream_t s, bool pdl) {
+  return launch_kernel(history_row_kernel, dim3(blocks(d.nxy(), 256)), dim3(256), 0, s, pdl, d.nxy(), T, layer, dz2,
+                       hist, ds);
 }
 
 cudaError_t launch_schedule_flags(const double* q, int64_t nrows, uint8_t* active, cudaStream_t s) {
@@ -585,12 +590,10 @@ cudaError_t launch_z_range(const StepArgs& a, const Coeffs& c, int64_t col_begin
   if (col_end <= col_begin) return cudaSuccess;
   const unsigned grid = blocks(col_end - col_begin, kLineThreads);
   if (a.z_discard)
-    sweep_z_kernel<true><<<grid, kLineThreads, 0, s>>>(d, a.W1, c.a2, c.b2, a.T_in, a.W0, a.T_out, col_begin, col_end,
-                                                        c.px);
-  else
-    sweep_z_kernel<false><<<grid, kLineThreads, 0, s>>>(d, a.W1, c.a2, c.b2, a.T_in, a.W0, a.T_out, col_begin,
-                                                         col_end, c.px);
-  return cudaGetLastError();
+    return launch_kernel(sweep_z_kernel<true>, dim3(grid), dim3(kLineThreads), 0, s, a.pdl, d, a.W1, c.a2, c.b2,
+                         a.T_in, a.W0, a.T_out, col_begin, col_end, c.px);
+  return launch_kernel(sweep_z_kernel<false>, dim3(grid), dim3(kLineThreads), 0, s, a.pdl, d, a.W1, c.a2, c.b2, a.T_in,
+                       a.W0, a.T_out, col_begin, col_end, c.px);
 }
 
 cudaError_t launch_copy_layer(const Dims& d, const double* T, int layer, double* dst, cudaStream_t s) {
