@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -246,6 +247,7 @@ __global__ void __launch_bounds__(kXT) adj_xsolve_kernel(AView v, const double* 
                                                          const double* __restrict__ M, const double* __restrict__ rhs,
                                                          const double* __restrict__ e, const double* __restrict__ u,
                                                          const double* __restrict__ ip, double* __restrict__ y) {
+  wait_prior_grid();  // the previous kernel on the stream (programmatic dependent launch)
   __shared__ double sc[kXL][kXC + 1], se[kXL][kXC + 1];
   const XGroup g = xgroup(v, blockIdx.x);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -337,6 +339,7 @@ __global__ void __launch_bounds__(128, kYMinBlocks) adj_ysolve_kernel(AView v, i
                                                                       const double* __restrict__ u,
                                                                       const double* __restrict__ ip, double* y,
                                                                       const double* T_in, double* T_out) {
+  wait_prior_grid();  // the previous kernel on the stream (programmatic dependent launch)
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= nlines) return;
   const Line ln = line_at(v, axis, t);
@@ -449,6 +452,7 @@ __global__ void __launch_bounds__(64) adj_ysolve_few_kernel(AView v, int axis, i
                                                             const double* __restrict__ u,
                                                             const double* __restrict__ ip, double* y,
                                                             const double* T_in, double* T_out) {
+  wait_prior_grid();  // the previous kernel on the stream (programmatic dependent launch)
   extern __shared__ double few_sm[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t t = blockIdx.x * (int64_t)32 + lane;
@@ -543,6 +547,7 @@ __global__ void adj_resid_kernel(AView v, const double* __restrict__ T, const do
                                  const double* __restrict__ gy, const double* __restrict__ gz,
                                  const double* __restrict__ D, const double* __restrict__ q, double s,
                                  double* __restrict__ r0) {
+  wait_prior_grid();  // the previous kernel on the stream (programmatic dependent launch)
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= v.nvox) return;
   const Vox x = vox_at(v, p);
@@ -586,6 +591,7 @@ __global__ void __launch_bounds__(128) adj_xsolve_few_kernel(AView v, int64_t ma
                                                              const double* rhs, const double* __restrict__ e,
                                                              const double* __restrict__ u,
                                                              const double* __restrict__ ip, double* y) {
+  wait_prior_grid();  // the previous kernel on the stream (programmatic dependent launch)
   extern __shared__ double few_sm[];
   const XGroup g = xgroup(v, blockIdx.x);
   // warp w solves the group's lines [lb, le): it copies them with lane = column and recurs with lane = line
@@ -671,6 +677,7 @@ __global__ void adj_update_kernel(AView v, const double* __restrict__ gx, const 
                                   const double* __restrict__ obs, int64_t obs_step, double* __restrict__ lam,
                                   double* __restrict__ ggx, double* __restrict__ ggy, double* __restrict__ ggz,
                                   double* __restrict__ gM, double* __restrict__ gq) {
+  wait_prior_grid();  // the previous kernel on the stream (programmatic dependent launch)
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= v.nvox) return;
   const Vox x = vox_at(v, p);
@@ -726,6 +733,7 @@ __device__ __forceinline__ double two_sum(double s, double v, double& err) {
 constexpr int kMisfitBlocks = 32;
 __global__ void adj_misfit_kernel(AView v, const double* __restrict__ T, const double* __restrict__ obs,
                                   int64_t step, double* __restrict__ part) {
+  wait_prior_grid();  // the previous kernel on the stream (programmatic dependent launch)
   __shared__ double sh_hi[256], sh_lo[256];
   const AInst& in = v.inst[blockIdx.y];
   const int64_t m = in.ny * in.nx;
@@ -873,6 +881,18 @@ namespace {
 
 using hs2g::kTh;
 using hs2g::nblk;
+using hs2g::launch_kernel;
+
+// The kernels of a step are launched with programmatic dependent launch (each waits for the previous kernel at its
+// start; no kernel triggers early): the launch latency at each kernel boundary is hidden.  HS2G_PDL=0 turns it
+// off.
+bool adj_pdl() {
+  static const bool on = [] {
+    const char* e = getenv("HS2G_PDL");
+    return !(e && strcmp(e, "0") == 0);
+  }();
+  return on;
+}
 
 int afail(int code, const char* m) { return hs2g::set_last_error(code, m); }
 int acuda(cudaError_t e, const char* what) {
@@ -932,8 +952,8 @@ template <bool HAS_M, bool ADD_T>
 void launch_ysolve(const hs2g::AView& v, cudaStream_t st, int axis, int64_t nl, const double* M, const double* rhs,
                    const double* e, const double* u, const double* ip, double* y, const double* T_in,
                    double* T_out) {
-  hs2g::adj_ysolve_kernel<HAS_M, ADD_T><<<line_blocks(nl), line_threads(nl), 0, st>>>(v, axis, nl, M, rhs, e, u, ip,
-                                                                                       y, T_in, T_out);
+  launch_kernel(hs2g::adj_ysolve_kernel<HAS_M, ADD_T>, dim3(line_blocks(nl)), dim3(line_threads(nl)), 0, st, adj_pdl(),
+                v, axis, nl, M, rhs, e, u, ip, y, T_in, T_out);
 }
 // y = A_a^-1 (M rhs) on the y or z lines (M null: A_a^-1 rhs); T_out = T_in + y when T_out is given
 void ysolve(hs2g_adjoint* a, cudaStream_t st, int axis, const double* M, const double* rhs, double* y,
@@ -945,15 +965,18 @@ void ysolve(hs2g_adjoint* a, cudaStream_t st, int axis, const double* M, const d
     const unsigned nbk = line_blocks(nl);
     const size_t sm = hs2g::few_smem_bytes(a->max_len[axis]);
     const int64_t ml = a->max_len[axis];
+#define HS2G_FEW(HM, AT)                                                                                      \
+  launch_kernel(hs2g::adj_ysolve_few_kernel<HM, AT>, dim3(nbk), dim3(64), sm, st, adj_pdl(), v, axis, nl, ml, M, rhs, \
+                e, u, ip, y, T_in, T_out)
     if (M && T_out)
-      hs2g::adj_ysolve_few_kernel<true, true><<<nbk, 64, sm, st>>>(v, axis, nl, ml, M, rhs, e, u, ip, y, T_in, T_out);
+      HS2G_FEW(true, true);
     else if (M)
-      hs2g::adj_ysolve_few_kernel<true, false><<<nbk, 64, sm, st>>>(v, axis, nl, ml, M, rhs, e, u, ip, y, T_in, T_out);
+      HS2G_FEW(true, false);
     else if (T_out)
-      hs2g::adj_ysolve_few_kernel<false, true><<<nbk, 64, sm, st>>>(v, axis, nl, ml, M, rhs, e, u, ip, y, T_in, T_out);
+      HS2G_FEW(false, true);
     else
-      hs2g::adj_ysolve_few_kernel<false, false><<<nbk, 64, sm, st>>>(v, axis, nl, ml, M, rhs, e, u, ip, y, T_in,
-                                                                      T_out);
+      HS2G_FEW(false, false);
+#undef HS2G_FEW
   } else if (M && T_out)
     launch_ysolve<true, true>(v, st, axis, nl, M, rhs, e, u, ip, y, T_in, T_out);
   else if (M)
@@ -969,12 +992,14 @@ cudaError_t fwd_step(hs2g_adjoint* a, cudaStream_t st, const double* T_in, doubl
                      double* y2, double s) {
   const hs2g::AView v = view(a);
   if (few_x(a)) {
-    hs2g::adj_resid_kernel<<<nblk(a->n), kTh, 0, st>>>(v, T_in, a->g[0], a->g[1], a->g[2], a->D, a->q, s, y0);
-    hs2g::adj_xsolve_few_kernel<false><<<(unsigned)a->nxgroups, 128, hs2g::few_x_smem_bytes(a->max_len[0], 3), st>>>(
-        v, a->max_len[0], nullptr, y0, a->e[0], a->u[0], a->ip[0], y0);
+    launch_kernel(hs2g::adj_resid_kernel, dim3(nblk(a->n)), dim3(kTh), 0, st, adj_pdl(), v, T_in, a->g[0], a->g[1],
+                  a->g[2], a->D, a->q, s, y0);
+    launch_kernel(hs2g::adj_xsolve_few_kernel<false>, dim3((unsigned)a->nxgroups), dim3(128),
+                  hs2g::few_x_smem_bytes(a->max_len[0], 3), st, adj_pdl(), v, a->max_len[0], nullptr, y0, a->e[0],
+                  a->u[0], a->ip[0], y0);
   } else {
-    hs2g::adj_xsolve_kernel<true><<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(
-        v, T_in, a->g[0], a->g[1], a->g[2], a->D, a->q, s, nullptr, nullptr, a->e[0], a->u[0], a->ip[0], y0);
+    launch_kernel(hs2g::adj_xsolve_kernel<true>, dim3((unsigned)a->nxgroups), dim3(hs2g::kXT), 0, st, adj_pdl(), v,
+                  T_in, a->g[0], a->g[1], a->g[2], a->D, a->q, s, nullptr, nullptr, a->e[0], a->u[0], a->ip[0], y0);
   }
   ysolve(a, st, 1, a->M, y0, y1, nullptr, nullptr);
   ysolve(a, st, 2, a->M, y1, y2, T_in, T_out);
@@ -990,15 +1015,16 @@ cudaError_t bwd_step(hs2g_adjoint* a, const double* Tn, const double* y0, const 
   ysolve(a, st, 2, nullptr, a->lam, a->mu[2], nullptr, nullptr);
   ysolve(a, st, 1, a->M, a->mu[2], a->mu[1], nullptr, nullptr);
   if (few_x(a))
-    hs2g::adj_xsolve_few_kernel<true><<<(unsigned)a->nxgroups, 128, hs2g::few_x_smem_bytes(a->max_len[0], 4), st>>>(
-        v, a->max_len[0], a->M, a->mu[1], a->e[0], a->u[0], a->ip[0], a->mu[0]);
+    launch_kernel(hs2g::adj_xsolve_few_kernel<true>, dim3((unsigned)a->nxgroups), dim3(128),
+                  hs2g::few_x_smem_bytes(a->max_len[0], 4), st, adj_pdl(), v, a->max_len[0], a->M, a->mu[1], a->e[0],
+                  a->u[0], a->ip[0], a->mu[0]);
   else
-    hs2g::adj_xsolve_kernel<false><<<(unsigned)a->nxgroups, hs2g::kXT, 0, st>>>(
-        v, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0.0, a->M, a->mu[1], a->e[0], a->u[0], a->ip[0],
-        a->mu[0]);
-  hs2g::adj_update_kernel<<<nblk(a->n), kTh, 0, st>>>(v, a->g[0], a->g[1], a->g[2], Tn, y0, y1, y2, a->mu[0],
-                                                      a->mu[1], a->mu[2], s, a->obs, obs_step, a->lam, a->gg[0],
-                                                      a->gg[1], a->gg[2], a->gM, a->gq);
+    launch_kernel(hs2g::adj_xsolve_kernel<false>, dim3((unsigned)a->nxgroups), dim3(hs2g::kXT), 0, st, adj_pdl(), v,
+                  nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0.0, a->M, a->mu[1], a->e[0], a->u[0],
+                  a->ip[0], a->mu[0]);
+  launch_kernel(hs2g::adj_update_kernel, dim3(nblk(a->n)), dim3(kTh), 0, st, adj_pdl(), v, a->g[0], a->g[1], a->g[2],
+                Tn, y0, y1, y2, a->mu[0], a->mu[1], a->mu[2], s, a->obs, obs_step, a->lam, a->gg[0], a->gg[1],
+                a->gg[2], a->gM, a->gq);
   return cudaGetLastError();
 }
 
@@ -1314,8 +1340,8 @@ int hs2g_adjoint_forward(hs2g_adjoint* a, int nsteps, const double* schedule, co
       if (e == cudaSuccess) e = fwd_step(a, st, slot, out, slot + n, slot + 2 * n, slot + 3 * n, a->sched[s]);
     }
     if (e == cudaSuccess) {
-      hs2g::adj_misfit_kernel<<<dim3(hs2g::kMisfitBlocks, a->ninst), 256, 0, st>>>(v, out, a->obs, s, a->parts);
-      e = cudaGetLastError();
+      e = launch_kernel(hs2g::adj_misfit_kernel, dim3(hs2g::kMisfitBlocks, a->ninst), dim3(256), 0, st, adj_pdl(), v,
+                        out, a->obs, (int64_t)s, a->parts);
     }
   }
   if (e == cudaSuccess) e = cudaEventRecord(a->ev1, st);
