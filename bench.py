@@ -53,16 +53,16 @@ FP64_OPS_PER_VOXEL = {"sweep_x": 9, "sweep_y": 2, "sweep_z": 3}
 KERNELS = ("sweep_x", "sweep_y", "sweep_z")
 # adjoint: arrays touched per voxel and step (8 B each), from the kernels of hs2g_adjoint.cu
 #   forward step (forward pass, and again as the recompute of the backward pass): x stage reads T, gx, gy, gz,
-#   D, q, lo0, ip0, u0 and writes y0 (10); y stage reads M, y0, lo1, ip1, u1, writes y1 (6); z stage reads M,
-#   y1, lo2, ip2, u2, T, writes y2, T' (8)                                                   -> 24 arrays
-#   reverse step: transposed z reads lambda, u2, lo2, ip2, writes mu2 (5); transposed y reads M, mu2, u1, lo1,
-#   ip1, writes mu1 (6); transposed x the same for mu0 (6); update reads gx, gy, gz, T, y0, y1, y2, mu0, mu1,
-#   mu2, lambda and the five accumulators and writes lambda and the accumulators (22)          -> 39 arrays
-# so one gradient evaluation moves (24 + 24 + 39) * 8 = 696 B (the x stage also reads the diagonal D) and does
-# about 20 + 20 + (3 + 4 + 4 + 34) = 85 FP64 operations per voxel and step (forward step, recompute,
+#   D, q, lo0, ip0, u0 and writes y0 (10); y stage reads y0, lo1, mip1, u1 (mip = M / piv), writes y1 (5); z stage
+#   reads y1, lo2, mip2, u2, T, writes y2, T' (7)                                             -> 22 arrays
+#   reverse step: transposed z reads lambda, u2, lo2, ip2, writes mu2 (5); transposed y reads mu2, u1, lo1,
+#   mip1, writes mu1 (5); transposed x the same for mu0 (5); update reads gx, gy, gz, T, y0, y1, y2, mu0, mu1,
+#   mu2, lambda and the five accumulators and writes lambda and the accumulators (22)          -> 37 arrays
+# so one gradient evaluation moves (22 + 22 + 37) * 8 = 648 B (the x stage also reads the diagonal D) and does
+# about 18 + 18 + (3 + 3 + 3 + 34) = 79 FP64 operations per voxel and step (forward step, recompute,
 # transposed solves and update).
-ADJ_BYTES_PER_VOXEL_STEP = (24 + 24 + 39) * 8
-ADJ_FP64_OPS_PER_VOXEL_STEP = 85
+ADJ_BYTES_PER_VOXEL_STEP = (22 + 22 + 37) * 8
+ADJ_FP64_OPS_PER_VOXEL_STEP = 79
 
 
 def parse_args():

@@ -168,10 +168,11 @@ __global__ void adj_diag_kernel(AView v, const double* __restrict__ gx, const do
 }
 
 // factors of A_a = M - L_a/2 per line, kept in the form the one-FMA-per-row recurrences of the solves use:
-// e = lo / piv (lo the sub-diagonal), u = (super-diagonal) / piv, ip = 1 / piv
+// e = lo / piv (lo the sub-diagonal), u = (super-diagonal) / piv, ip = 1 / piv, mip = M / piv (the scale of
+// the stages whose right-hand side is M rhs)
 __global__ void adj_factor_kernel(AView v, int axis, int64_t nlines, const double* __restrict__ M,
                                   const double* __restrict__ g, double* __restrict__ e, double* __restrict__ u,
-                                  double* __restrict__ ip) {
+                                  double* __restrict__ ip, double* __restrict__ mip) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= nlines) return;
   const Line ln = line_at(v, axis, t);
@@ -187,17 +188,19 @@ __global__ void adj_factor_kernel(AView v, int axis, int64_t nlines, const doubl
     e[p] = l * inv;
     u[p] = uu;
     ip[p] = inv;
+    mip[p] = __dmul_rn(M[p], inv);
     u_prev = uu;
   }
 }
 
 // Every line solve below is y = A_a^-1 b with A_a = Lo U (Lo: pivots on the diagonal, lo below; U: unit
 // diagonal, u above) in two passes of one dependent FMA per row:
-//     z_r = fma(-e_r, z_{r-1}, c_r),  c_r = b_r * ip_r     (rows ascending)
+//     z_r = fma(-e_r, z_{r-1}, c_r),  c_r = rhs_r * s_r       (rows ascending)
 //     y_r = fma(-u_r, y_{r+1}, z_r)                           (rows descending)
-// with b = M rhs (or rhs itself, or the residual r0 in the forward x stage).  The rounding of every operation
-// is explicit (no contraction left to the compiler), so the register-blocked kernels for many lines and the
-// shared-memory few-line kernels give the same bits.
+// with b = M rhs and s = mip = M / piv for the stages weighted by M (one multiplication per row instead of
+// two), b = rhs and s = ip = 1 / piv otherwise (the residual r0 in the forward x stage, lambda in the first
+// adjoint stage).  The rounding of every operation is explicit (no contraction left to the compiler), so the
+// register-blocked kernels for many lines and the shared-memory few-line kernels give the same bits.
 
 // The x-line kernels below stage 32 lines x 32 columns of each operand through shared memory: loads and
 // stores are row-contiguous (lane = column), the recurrence runs one line per lane of warp 0 (lane = line).
@@ -237,16 +240,16 @@ __device__ __forceinline__ double residual_at(const double* __restrict__ T, cons
   return r;
 }
 
-// x stage: y = A_x^-1 b.  RESID: b = the residual r0 = L T + s q (the forward step's first stage, fused);
-// otherwise b = M rhs (the adjoint's last stage, mu0 = A_x^-1 (M mu1)).
+// x stage: y = A_x^-1 b.  RESID: b = the residual r0 = L T + s q (the forward step's first stage, fused),
+// scale = ip; otherwise b = M rhs (the adjoint's last stage, mu0 = A_x^-1 (M mu1)), scale = mip.
 template <bool RESID>
 __global__ void __launch_bounds__(kXT) adj_xsolve_kernel(AView v, const double* __restrict__ T,
                                                          const double* __restrict__ gx, const double* __restrict__ gy,
                                                          const double* __restrict__ gz, const double* __restrict__ D,
                                                          const double* __restrict__ q, double s,
-                                                         const double* __restrict__ M, const double* __restrict__ rhs,
-                                                         const double* __restrict__ e, const double* __restrict__ u,
-                                                         const double* __restrict__ ip, double* __restrict__ y) {
+                                                         const double* __restrict__ rhs, const double* __restrict__ e,
+                                                         const double* __restrict__ u,
+                                                         const double* __restrict__ scale, double* __restrict__ y) {
   wait_prior_grid();  // the previous kernel on the stream (programmatic dependent launch)
   __shared__ double sc[kXL][kXC + 1], se[kXL][kXC + 1];
   const XGroup g = xgroup(v, blockIdx.x);
@@ -264,12 +267,9 @@ __global__ void __launch_bounds__(kXT) adj_xsolve_kernel(AView v, const double* 
       if (l < g.nl && i < g.nx) {
         const int64_t line = g.l0 + l;
         const int64_t p = g.off + line * g.nx + i;
-        double b;
-        if (RESID)
-          b = residual_at(T, gx, gy, gz, D, q, s, p, i, line % g.ny, line / g.ny, g.nx, g.ny, g.nz);
-        else
-          b = __dmul_rn(M[p], rhs[p]);
-        sc[l][lane] = __dmul_rn(b, ip[p]);
+        const double b =
+            RESID ? residual_at(T, gx, gy, gz, D, q, s, p, i, line % g.ny, line / g.ny, g.nx, g.ny, g.nz) : rhs[p];
+        sc[l][lane] = __dmul_rn(b, scale[p]);
         se[l][lane] = e[p];
       }
     }
@@ -320,7 +320,8 @@ __global__ void __launch_bounds__(kXT) adj_xsolve_kernel(AView v, const double* 
   }
 }
 
-// y / z stage: y = A_a^-1 (M rhs) along each strided line (M null: A_a^-1 rhs), one thread per line,
+// y / z stage: y = A_a^-1 b along each strided line, c_r = rhs_r * scale_r (scale = mip for b = M rhs, ip for
+// b = rhs), one thread per line,
 // neighbouring threads on neighbouring lines, so every row access is coalesced; T_out = T_in + y when T_out
 // is given (T_out may equal T_in).  Rows go in blocks of kRB: the loads of a block are issued together, then
 // the recurrence runs through it, so a line pays one memory latency per block instead of one per row.
@@ -331,13 +332,12 @@ __global__ void __launch_bounds__(kXT) adj_xsolve_kernel(AView v, const double* 
 constexpr int kRB = 4;
 constexpr int kYMinBlocks = 12;
 
-template <bool HAS_M, bool ADD_T>
+template <bool ADD_T>
 __global__ void __launch_bounds__(128, kYMinBlocks) adj_ysolve_kernel(AView v, int axis, int64_t nlines,
-                                                                      const double* __restrict__ M,
                                                                       const double* rhs,
                                                                       const double* __restrict__ e,
                                                                       const double* __restrict__ u,
-                                                                      const double* __restrict__ ip, double* y,
+                                                                      const double* __restrict__ scale, double* y,
                                                                       const double* T_in, double* T_out) {
   wait_prior_grid();  // the previous kernel on the stream (programmatic dependent launch)
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -354,8 +354,7 @@ __global__ void __launch_bounds__(128, kYMinBlocks) adj_ysolve_kernel(AView v, i
     for (int k = 0; k < kRB; ++k) {
       if (r0 + k < len) {
         const uint32_t p = o + k * stride;
-        const double b = HAS_M ? __dmul_rn(M[p], rhs[p]) : rhs[p];
-        c[k] = __dmul_rn(b, ip[p]);
+        c[k] = __dmul_rn(rhs[p], scale[p]);
         ee[k] = e[p];
       }
     }
@@ -417,7 +416,7 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// dynamic shared memory of a few-line launch: the line values, then the ring of up to 4 operands
+// dynamic shared memory of a few-line launch: the line values, then the ring (room for 4 operands, 3 used)
 inline size_t few_smem_bytes(int64_t max_len) {
   return sizeof(double) * 32 * (size_t)(max_len + kFS * kFR * 4);
 }
@@ -438,19 +437,22 @@ __device__ __forceinline__ void named_bar_arrive(int id, int nthreads) {
   asm volatile("bar.arrive %0, %1;\n" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-// Two warps per CTA over the same 32 lines (lane = line): warp 1 issues the copies, warp 0 runs the
-// recurrence.  Ring slot s is handed over with named barriers, FULL(s) = 1 + s from producer to consumer once
-// the slot's copies have landed, EMPTY(s) = 1 + kFS + s back once it is consumed.  Both warps count the blocks
-// of the two passes as one sequence q = 0 .. 2 nb - 1 (nb = blocks of the CTA's longest line), slot q % kFS,
-// and run the same barrier sequence whatever their lines' lengths, so every barrier is met.
+// Two warps per CTA over the same 32 lines (lane = line): warp 1 issues the copies and forms each forward row's
+// scaled right-hand side c = rhs * scale once the row has landed, warp 0 runs the recurrence.  A warp issues
+// one FP64 instruction per 64 cycles on GB300 (the measured latency of a dependent FMA is the same 64 cycles),
+// so the multiplications that do not depend on the recurrence run on the copying warp's sub-partition while the
+// recurrence warp issues only its chained FMAs.  Ring slot s is handed over with named barriers, FULL(s) = 1 + s
+// from producer to consumer once the slot's copies have landed and its c values are written, EMPTY(s) =
+// 1 + kFS + s back once it is consumed.  Both warps count the blocks of the two passes as one sequence
+// q = 0 .. 2 nb - 1 (nb = blocks of the CTA's longest line), slot q % kFS, and run the same barrier sequence
+// whatever their lines' lengths, so every barrier is met.
 constexpr int kFewLag = 2;  // blocks the producer keeps in flight before handing the oldest over
 
-template <bool HAS_M, bool ADD_T>
+template <bool ADD_T>
 __global__ void __launch_bounds__(64) adj_ysolve_few_kernel(AView v, int axis, int64_t nlines, int64_t max_len,
-                                                            const double* __restrict__ M, const double* rhs,
-                                                            const double* __restrict__ e,
+                                                            const double* rhs, const double* __restrict__ e,
                                                             const double* __restrict__ u,
-                                                            const double* __restrict__ ip, double* y,
+                                                            const double* __restrict__ scale, double* y,
                                                             const double* T_in, double* T_out) {
   wait_prior_grid();  // the previous kernel on the stream (programmatic dependent launch)
   extern __shared__ double few_sm[];
@@ -462,8 +464,17 @@ __global__ void __launch_bounds__(64) adj_ysolve_few_kernel(AView v, int axis, i
   const int len = (int)ln.len;
   const int nb = __reduce_max_sync(0xffffffffu, (len + kFR - 1) / kFR), nq = 2 * nb;
   if (warp == 1) {
-    // producer: block q < nb is rows [q kFR, q kFR + kFR) ascending (rhs, e, ip, M), block q >= nb rows
-    // len - 1 - (q - nb) kFR - k descending (u, T_in)
+    // producer: block q < nb is rows [q kFR, q kFR + kFR) ascending (rhs, e, scale; rhs replaced by c once
+    // landed), block q >= nb rows len - 1 - (q - nb) kFR - k descending (u, T_in)
+    auto hand_over = [&](int qq) {  // block qq has landed (this thread's copies): form c, then release the slot
+      if (qq < nb) {
+#pragma unroll
+        for (int k = 0; k < kFR; ++k)
+          if (qq * kFR + k < len) *R.at(qq, k, 0) = __dmul_rn(*R.at(qq, k, 0), *R.at(qq, k, 2));
+      }
+      __threadfence_block();
+      named_bar_arrive(1 + qq % kFS, 64);
+    };
     for (int q = 0; q < nq; ++q) {
       if (q >= kFS) named_bar_sync(1 + kFS + q % kFS, 64);  // the consumer is done with block q - kFS
 #pragma unroll
@@ -474,8 +485,7 @@ __global__ void __launch_bounds__(64) adj_ysolve_few_kernel(AView v, int axis, i
             const int64_t p = ln.base + r * ln.stride;
             cp_async8(R.at(q, k, 0), rhs + p);
             cp_async8(R.at(q, k, 1), e + p);
-            cp_async8(R.at(q, k, 2), ip + p);
-            if (HAS_M) cp_async8(R.at(q, k, 3), M + p);
+            cp_async8(R.at(q, k, 2), scale + p);
           }
         } else {
           const int r = len - 1 - ((q - nb) * kFR + k);
@@ -489,13 +499,11 @@ __global__ void __launch_bounds__(64) adj_ysolve_few_kernel(AView v, int axis, i
       cp_async_commit();
       if (q >= kFewLag) {
         cp_async_wait<kFewLag>();  // block q - kFewLag has landed
-        __threadfence_block();
-        named_bar_arrive(1 + (q - kFewLag) % kFS, 64);
+        hand_over(q - kFewLag);
       }
     }
     cp_async_wait<0>();
-    __threadfence_block();
-    for (int q = nq > kFewLag ? nq - kFewLag : 0; q < nq; ++q) named_bar_arrive(1 + q % kFS, 64);
+    for (int q = nq > kFewLag ? nq - kFewLag : 0; q < nq; ++q) hand_over(q);
     return;
   }
   double z = 0.0, x = 0.0;
@@ -506,8 +514,7 @@ __global__ void __launch_bounds__(64) adj_ysolve_few_kernel(AView v, int axis, i
       for (int k = 0; k < kFR; ++k) {
         const int r = q * kFR + k;
         if (r < len) {
-          const double b = HAS_M ? __dmul_rn(*R.at(q, k, 3), *R.at(q, k, 0)) : *R.at(q, k, 0);
-          z = __fma_rn(-*R.at(q, k, 1), z, __dmul_rn(b, *R.at(q, k, 2)));
+          z = __fma_rn(-*R.at(q, k, 1), z, *R.at(q, k, 0));
           line[r * 32 + lane] = z;
         }
       }
@@ -534,10 +541,10 @@ __global__ void __launch_bounds__(64) adj_ysolve_few_kernel(AView v, int axis, i
 // memory between the two passes and stores them once, row-contiguous.  The forward stage's residual r0 comes
 // from adj_resid_kernel (one thread per voxel) instead of being fused.  Same operations, same order, same
 // rounding as adj_xsolve_kernel.
-constexpr int kXFS = 3;              // ring stages (tiles of kXL lines x kXC columns x up to 4 operands)
+constexpr int kXFS = 3;              // ring stages (tiles of kXL lines x kXC columns x 3 operands)
 constexpr int kFewLanes = 8;         // lines per warp (four warps per group: the copies spread over them)
 constexpr int kFewXGroups = 2 * 152; // at most this many 32-line groups
-constexpr int kFewMaxNx = 448;       // longest x-line the few-line kernel holds (4 operands: 211 KB)
+constexpr int kFewMaxNx = 448;       // longest x-line the few-line kernel holds (187 KB of shared memory)
 
 inline size_t few_x_smem_bytes(int64_t max_nx, int nops) {
   return sizeof(double) * ((size_t)kXL * (size_t)(max_nx + 1) + (size_t)kXFS * nops * kXL * (kXC + 1));
@@ -585,37 +592,42 @@ __device__ __forceinline__ void few_x_issue(const FewX& F, const XGroup& g, int 
   cp_async_commit();
 }
 
-// y = A_x^-1 (M rhs) (HAS_M), or A_x^-1 rhs (rhs = r0 in the forward stage; rhs may alias y)
-template <bool HAS_M>
-__global__ void __launch_bounds__(128) adj_xsolve_few_kernel(AView v, int64_t max_nx, const double* __restrict__ M,
-                                                             const double* rhs, const double* __restrict__ e,
+// y = A_x^-1 b with c = rhs * scale: scale = mip for b = M rhs (the adjoint's last stage), ip for b = rhs (the
+// forward stage's residual r0; rhs may alias y)
+__global__ void __launch_bounds__(128) adj_xsolve_few_kernel(AView v, int64_t max_nx, const double* rhs,
+                                                             const double* __restrict__ e,
                                                              const double* __restrict__ u,
-                                                             const double* __restrict__ ip, double* y) {
+                                                             const double* __restrict__ scale, double* y) {
   wait_prior_grid();  // the previous kernel on the stream (programmatic dependent launch)
   extern __shared__ double few_sm[];
   const XGroup g = xgroup(v, blockIdx.x);
   // warp w solves the group's lines [lb, le): it copies them with lane = column and recurs with lane = line
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int lb = min(warp * kFewLanes, (int)g.nl), le = min(lb + kFewLanes, (int)g.nl), ln = lb + lane;
-  const FewX F{few_sm, few_sm + kXL * (max_nx + 1), max_nx + 1, HAS_M ? 4 : 3};
-  const double* Mop = HAS_M ? M : nullptr;
+  const FewX F{few_sm, few_sm + kXL * (max_nx + 1), max_nx + 1, 3};
   const int nch = (int)((g.nx + kXC - 1) / kXC);
-  for (int q = 0; q < kXFS - 1; ++q) few_x_issue(F, g, q, q < nch ? q : -1, lane, lb, le, rhs, e, ip, Mop);
+  for (int q = 0; q < kXFS - 1; ++q) few_x_issue(F, g, q, q < nch ? q : -1, lane, lb, le, rhs, e, scale, nullptr);
   double z = 0.0;
   for (int ch = 0; ch < nch; ++ch) {
     __syncwarp();  // every lane is done with the slot refilled here
     const int nxt = ch + kXFS - 1;
-    few_x_issue(F, g, nxt, nxt < nch ? nxt : -1, lane, lb, le, rhs, e, ip, Mop);
+    few_x_issue(F, g, nxt, nxt < nch ? nxt : -1, lane, lb, le, rhs, e, scale, nullptr);
     cp_async_wait<kXFS - 1>();
     __syncwarp();  // chunk ch's copies by every lane are visible
+    // c = rhs * scale with lane = column, one multiplication per 32 columns, before the recurrence (lane = line,
+    // kFewLanes lines per warp) runs its chained FMAs alone
+    if ((int64_t)ch * kXC + lane < g.nx)
+      for (int l = lb; l < le; ++l) {
+        double* tb = F.tile(ch, 0, l) + lane;
+        *tb = __dmul_rn(*tb, F.tile(ch, 2, l)[lane]);
+      }
+    __syncwarp();
     if (ln < le) {
       const int cw = (int)min((int64_t)kXC, g.nx - (int64_t)ch * kXC);
-      const double *tb = F.tile(ch, 0, ln), *te = F.tile(ch, 1, ln), *ti = F.tile(ch, 2, ln);
-      const double* tm = HAS_M ? F.tile(ch, 3, ln) : tb;
+      const double *tc = F.tile(ch, 0, ln), *te = F.tile(ch, 1, ln);
       double* zr = F.lines + ln * F.zs + ch * kXC;
       auto step = [&](int cc) {
-        const double b = HAS_M ? __dmul_rn(tm[cc], tb[cc]) : tb[cc];
-        z = __fma_rn(-te[cc], z, __dmul_rn(b, ti[cc]));
+        z = __fma_rn(-te[cc], z, tc[cc]);
         zr[cc] = z;
       };
       if (cw == kXC) {
@@ -854,9 +866,9 @@ struct hs2g_adjoint {
   double* forms = nullptr;   // [ninst][nclass][3][3]
   int nclass = 0;
   int* err = nullptr;
-  // line factors of A_x, A_y, A_z: e = lo / piv, u = super-diagonal / piv, ip = 1 / piv
+  // line factors of A_x, A_y, A_z: e = lo / piv, u = super-diagonal / piv, ip = 1 / piv, mip = M / piv
   double *e[3] = {nullptr, nullptr, nullptr}, *u[3] = {nullptr, nullptr, nullptr},
-         *ip[3] = {nullptr, nullptr, nullptr};
+         *ip[3] = {nullptr, nullptr, nullptr}, *mip[3] = {nullptr, nullptr, nullptr};
   // run state
   bool have_params = false;
   int nsteps = 0, ckpt = 1;
@@ -948,43 +960,33 @@ bool few_lines(const hs2g_adjoint* a, int axis) {
 bool few_x(const hs2g_adjoint* a) {
   return a->nxgroups <= hs2g::kFewXGroups && a->max_len[0] <= hs2g::kFewMaxNx;
 }
-template <bool HAS_M, bool ADD_T>
-void launch_ysolve(const hs2g::AView& v, cudaStream_t st, int axis, int64_t nl, const double* M, const double* rhs,
-                   const double* e, const double* u, const double* ip, double* y, const double* T_in,
-                   double* T_out) {
-  launch_kernel(hs2g::adj_ysolve_kernel<HAS_M, ADD_T>, dim3(line_blocks(nl)), dim3(line_threads(nl)), 0, st, adj_pdl(),
-                v, axis, nl, M, rhs, e, u, ip, y, T_in, T_out);
+template <bool ADD_T>
+void launch_ysolve(const hs2g::AView& v, cudaStream_t st, int axis, int64_t nl, const double* rhs, const double* e,
+                   const double* u, const double* scale, double* y, const double* T_in, double* T_out) {
+  launch_kernel(hs2g::adj_ysolve_kernel<ADD_T>, dim3(line_blocks(nl)), dim3(line_threads(nl)), 0, st, adj_pdl(), v,
+                axis, nl, rhs, e, u, scale, y, T_in, T_out);
 }
-// y = A_a^-1 (M rhs) on the y or z lines (M null: A_a^-1 rhs); T_out = T_in + y when T_out is given
-void ysolve(hs2g_adjoint* a, cudaStream_t st, int axis, const double* M, const double* rhs, double* y,
+// y = A_a^-1 (M rhs) on the y or z lines (weighted false: A_a^-1 rhs); T_out = T_in + y when T_out is given
+void ysolve(hs2g_adjoint* a, cudaStream_t st, int axis, bool weighted, const double* rhs, double* y,
             const double* T_in, double* T_out) {
   const hs2g::AView v = view(a);
   const int64_t nl = a->nlines[axis];
-  const double *e = a->e[axis], *u = a->u[axis], *ip = a->ip[axis];
+  const double *e = a->e[axis], *u = a->u[axis], *scale = weighted ? a->mip[axis] : a->ip[axis];
   if (few_lines(a, axis)) {
     const unsigned nbk = line_blocks(nl);
     const size_t sm = hs2g::few_smem_bytes(a->max_len[axis]);
     const int64_t ml = a->max_len[axis];
-#define HS2G_FEW(HM, AT)                                                                                      \
-  launch_kernel(hs2g::adj_ysolve_few_kernel<HM, AT>, dim3(nbk), dim3(64), sm, st, adj_pdl(), v, axis, nl, ml, M, rhs, \
-                e, u, ip, y, T_in, T_out)
-    if (M && T_out)
-      HS2G_FEW(true, true);
-    else if (M)
-      HS2G_FEW(true, false);
-    else if (T_out)
-      HS2G_FEW(false, true);
+    if (T_out)
+      launch_kernel(hs2g::adj_ysolve_few_kernel<true>, dim3(nbk), dim3(64), sm, st, adj_pdl(), v, axis, nl, ml, rhs,
+                    e, u, scale, y, T_in, T_out);
     else
-      HS2G_FEW(false, false);
-#undef HS2G_FEW
-  } else if (M && T_out)
-    launch_ysolve<true, true>(v, st, axis, nl, M, rhs, e, u, ip, y, T_in, T_out);
-  else if (M)
-    launch_ysolve<true, false>(v, st, axis, nl, M, rhs, e, u, ip, y, T_in, T_out);
-  else if (T_out)
-    launch_ysolve<false, true>(v, st, axis, nl, M, rhs, e, u, ip, y, T_in, T_out);
-  else
-    launch_ysolve<false, false>(v, st, axis, nl, M, rhs, e, u, ip, y, T_in, T_out);
+      launch_kernel(hs2g::adj_ysolve_few_kernel<false>, dim3(nbk), dim3(64), sm, st, adj_pdl(), v, axis, nl, ml, rhs,
+                    e, u, scale, y, T_in, T_out);
+  } else if (T_out) {
+    launch_ysolve<true>(v, st, axis, nl, rhs, e, u, scale, y, T_in, T_out);
+  } else {
+    launch_ysolve<false>(v, st, axis, nl, rhs, e, u, scale, y, T_in, T_out);
+  }
 }
 
 // one forward step T_in -> T_out on stream st keeping y0, y1, y2 (T_out may alias T_in; NULL skips it)
@@ -994,15 +996,15 @@ cudaError_t fwd_step(hs2g_adjoint* a, cudaStream_t st, const double* T_in, doubl
   if (few_x(a)) {
     launch_kernel(hs2g::adj_resid_kernel, dim3(nblk(a->n)), dim3(kTh), 0, st, adj_pdl(), v, T_in, a->g[0], a->g[1],
                   a->g[2], a->D, a->q, s, y0);
-    launch_kernel(hs2g::adj_xsolve_few_kernel<false>, dim3((unsigned)a->nxgroups), dim3(128),
-                  hs2g::few_x_smem_bytes(a->max_len[0], 3), st, adj_pdl(), v, a->max_len[0], nullptr, y0, a->e[0],
-                  a->u[0], a->ip[0], y0);
+    launch_kernel(hs2g::adj_xsolve_few_kernel, dim3((unsigned)a->nxgroups), dim3(128),
+                  hs2g::few_x_smem_bytes(a->max_len[0], 3), st, adj_pdl(), v, a->max_len[0], y0, a->e[0], a->u[0],
+                  a->ip[0], y0);
   } else {
     launch_kernel(hs2g::adj_xsolve_kernel<true>, dim3((unsigned)a->nxgroups), dim3(hs2g::kXT), 0, st, adj_pdl(), v,
-                  T_in, a->g[0], a->g[1], a->g[2], a->D, a->q, s, nullptr, nullptr, a->e[0], a->u[0], a->ip[0], y0);
+                  T_in, a->g[0], a->g[1], a->g[2], a->D, a->q, s, nullptr, a->e[0], a->u[0], a->ip[0], y0);
   }
-  ysolve(a, st, 1, a->M, y0, y1, nullptr, nullptr);
-  ysolve(a, st, 2, a->M, y1, y2, T_in, T_out);
+  ysolve(a, st, 1, true, y0, y1, nullptr, nullptr);
+  ysolve(a, st, 2, true, y1, y2, T_in, T_out);
   return cudaGetLastError();
 }
 
@@ -1012,16 +1014,16 @@ cudaError_t bwd_step(hs2g_adjoint* a, const double* Tn, const double* y0, const 
                      double s, int64_t obs_step) {
   const hs2g::AView v = view(a);
   cudaStream_t st = a->stream;
-  ysolve(a, st, 2, nullptr, a->lam, a->mu[2], nullptr, nullptr);
-  ysolve(a, st, 1, a->M, a->mu[2], a->mu[1], nullptr, nullptr);
+  ysolve(a, st, 2, false, a->lam, a->mu[2], nullptr, nullptr);
+  ysolve(a, st, 1, true, a->mu[2], a->mu[1], nullptr, nullptr);
   if (few_x(a))
-    launch_kernel(hs2g::adj_xsolve_few_kernel<true>, dim3((unsigned)a->nxgroups), dim3(128),
-                  hs2g::few_x_smem_bytes(a->max_len[0], 4), st, adj_pdl(), v, a->max_len[0], a->M, a->mu[1], a->e[0],
-                  a->u[0], a->ip[0], a->mu[0]);
+    launch_kernel(hs2g::adj_xsolve_few_kernel, dim3((unsigned)a->nxgroups), dim3(128),
+                  hs2g::few_x_smem_bytes(a->max_len[0], 3), st, adj_pdl(), v, a->max_len[0], a->mu[1], a->e[0],
+                  a->u[0], a->mip[0], a->mu[0]);
   else
     launch_kernel(hs2g::adj_xsolve_kernel<false>, dim3((unsigned)a->nxgroups), dim3(hs2g::kXT), 0, st, adj_pdl(), v,
-                  nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0.0, a->M, a->mu[1], a->e[0], a->u[0],
-                  a->ip[0], a->mu[0]);
+                  nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0.0, a->mu[1], a->e[0], a->u[0], a->mip[0],
+                  a->mu[0]);
   launch_kernel(hs2g::adj_update_kernel, dim3(nblk(a->n)), dim3(kTh), 0, st, adj_pdl(), v, a->g[0], a->g[1], a->g[2],
                 Tn, y0, y1, y2, a->mu[0], a->mu[1], a->mu[2], s, a->obs, obs_step, a->lam, a->gg[0], a->gg[1],
                 a->gg[2], a->gM, a->gq);
@@ -1031,6 +1033,7 @@ cudaError_t bwd_step(hs2g_adjoint* a, const double* Tn, const double* y0, const 
 void adj_free(hs2g_adjoint* a) {
   void* ptrs[] = {a->inst, a->vox_off, a->line_off, a->xg_off, a->k, a->C, a->q, a->M, a->D, a->g[0], a->g[1],
                   a->g[2], a->e[0], a->e[1], a->e[2], a->u[0], a->u[1], a->u[2], a->ip[0], a->ip[1], a->ip[2],
+                  a->mip[0], a->mip[1], a->mip[2],
                   a->obs, a->ckpts, a->seg, a->seg2, a->T, a->lam, a->mu[0], a->mu[1], a->mu[2], a->gg[0], a->gg[1],
                   a->gg[2], a->gM, a->gq, a->parts, a->fcls, a->fixed, a->forms, a->err};
   for (void* p : ptrs)
@@ -1090,7 +1093,7 @@ int hs2g_adjoint_create(int n, const hs2g_adjoint_grid* grids, double dt, int de
     xg_off[i + 1] = xg_off[i] + (g.nz * g.ny + hs2g::kXL - 1) / hs2g::kXL;
   }
   if (xg_off[n] > 0x7fffffff) return afail(HS2G_ERR_ARG, "hs2g_adjoint_create: batch too large");
-  // the line kernels index voxels with 32 bits; 2^31 voxels would need 464 GB for the 27 per-voxel fields
+  // the line kernels index voxels with 32 bits; 2^31 voxels would need 515 GB for the 30 per-voxel fields
   if (vox_off[n] > 0x7fffffff) return afail(HS2G_ERR_ARG, "hs2g_adjoint_create: batch too large (2^31 voxels)");
   AGuard guard(device);
   if (!guard.ok) return afail(HS2G_ERR_CUDA, "hs2g_adjoint_create: cannot select device");
@@ -1119,27 +1122,23 @@ int hs2g_adjoint_create(int n, const hs2g_adjoint_grid* grids, double dt, int de
   }
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&a->ev_start, cudaEventDisableTiming);
   {
-    const void* few_y[] = {(const void*)hs2g::adj_ysolve_few_kernel<true, true>,
-                           (const void*)hs2g::adj_ysolve_few_kernel<true, false>,
-                           (const void*)hs2g::adj_ysolve_few_kernel<false, true>,
-                           (const void*)hs2g::adj_ysolve_few_kernel<false, false>};
+    const void* few_y[] = {(const void*)hs2g::adj_ysolve_few_kernel<true>,
+                           (const void*)hs2g::adj_ysolve_few_kernel<false>};
     for (const void* f : few_y)
       if (e == cudaSuccess)
         e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)hs2g::few_smem_bytes(hs2g::kFewMaxLen));
   }
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(hs2g::adj_xsolve_few_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)hs2g::few_x_smem_bytes(hs2g::kFewMaxNx, 4));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(hs2g::adj_xsolve_few_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(hs2g::adj_xsolve_few_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)hs2g::few_x_smem_bytes(hs2g::kFewMaxNx, 3));
   if (e == cudaSuccess) e = cudaMalloc(&a->inst, sizeof(hs2g::AInst) * n);
   if (e == cudaSuccess) e = cudaMalloc(&a->vox_off, sizeof(int64_t) * (n + 1));
   if (e == cudaSuccess) e = cudaMalloc(&a->line_off, sizeof(int64_t) * 3 * (n + 1));
   if (e == cudaSuccess) e = cudaMalloc(&a->xg_off, sizeof(int64_t) * (n + 1));
   double** per_voxel[] = {&a->k, &a->C, &a->q, &a->M, &a->D, &a->g[0], &a->g[1], &a->g[2], &a->e[0], &a->e[1],
-                          &a->e[2], &a->u[0], &a->u[1], &a->u[2], &a->ip[0], &a->ip[1], &a->ip[2], &a->T,
+                          &a->e[2], &a->u[0], &a->u[1], &a->u[2], &a->ip[0], &a->ip[1], &a->ip[2], &a->mip[0],
+                          &a->mip[1], &a->mip[2], &a->T,
                           &a->lam, &a->mu[0], &a->mu[1], &a->mu[2], &a->gg[0], &a->gg[1], &a->gg[2], &a->gM,
                           &a->gq};
   const int nfields = (int)(sizeof(per_voxel) / sizeof(per_voxel[0]));
@@ -1217,7 +1216,7 @@ int hs2g_adjoint_set_parameters(hs2g_adjoint* a, const double* k, const double* 
   hs2g::adj_diag_kernel<<<nblk(n), kTh, 0, st>>>(v, a->g[0], a->g[1], a->g[2], a->D);
   for (int ax = 0; ax < 3; ++ax)
     hs2g::adj_factor_kernel<<<nblk(a->nlines[ax]), kTh, 0, st>>>(v, ax, a->nlines[ax], a->M, a->g[ax], a->e[ax],
-                                                                a->u[ax], a->ip[ax]);
+                                                                a->u[ax], a->ip[ax], a->mip[ax]);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return acuda(e, "hs2g_adjoint_set_parameters");

@@ -69,11 +69,14 @@ def factor(M, g, axis):
     return tuple(np.moveaxis(a, -1, axis) for a in (e, u, ip))
 
 
-def solve(f, b, axis):
+def solve(f, b, axis, M=None):
     """A^-1 b along `axis` in the two one-FMA passes of the device's line solves:
     z_r = c_r - e_r z_{r-1} with c_r = b_r ip_r (ascending), y_r = z_r - u_r y_{r+1} (descending).
+    With M: A^-1 (M b), c_r = b_r (M_r ip_r), M / piv formed once as adj_factor_kernel's mip.
     A is symmetric, so the adjoint's transposed solves are this solve too."""
     e, u, ip = (np.moveaxis(a, axis, -1) for a in f)
+    if M is not None:
+        ip = np.moveaxis(M, axis, -1) * ip
     bt = np.moveaxis(b, axis, -1)
     n = bt.shape[-1]
     y = np.zeros_like(bt)
@@ -136,8 +139,8 @@ class Model(object):
     def fwd_step(self, T, s):
         gz, gy, gx = self.g
         y0 = solve(self.f[0], residual(T, self.q, s, gz, gy, gx, self.D), 2)
-        y1 = solve(self.f[1], self.M * y0, 1)
-        y2 = solve(self.f[2], self.M * y1, 0)
+        y1 = solve(self.f[1], y0, 1, self.M)
+        y2 = solve(self.f[2], y1, 0, self.M)
         return T + y2, y0, y1, y2
 
     def forward(self, T0, schedule, obs, ckpt):
@@ -172,8 +175,8 @@ class Model(object):
             for s in range(s1 - 1, s0 - 1, -1):
                 Tn, y0, y1, y2 = slots[s - s0]
                 mu2 = solve(self.f[2], lam, 0)
-                mu1 = solve(self.f[1], self.M * mu2, 1)
-                mu0 = solve(self.f[0], self.M * mu1, 2)
+                mu1 = solve(self.f[1], mu2, 1, self.M)
+                mu0 = solve(self.f[0], mu1, 2, self.M)
                 lam = lam + lap(mu0, gz, gy, gx)
                 if s >= 1:
                     lam[0] += 2.0 * (Tn[0] - self.obs[s - 1])
