@@ -46,23 +46,26 @@ constexpr int kLineThreads = 128;
 // A sweep's forward values are written and read back by the same thread block within microseconds; with
 // every line in flight they add up to more than L2 (136 MB at 65x512x512), so they are stored with an
 // evict-last L2 policy where that keeps them on chip.
-template <bool HAS_Q>
+// IX: the index type of the voxel, line and coefficient-block arithmetic (int32_t when the grid and its stencil
+// blocks have fewer than 2^31 elements, which makes the line -> (k, j) division a 32-bit one).
+template <bool HAS_Q, typename IX = int64_t>
 __device__ __forceinline__ double stencil_x(const Dims& d, const double* __restrict__ T, const Coeffs& c,
                                             const uint8_t* __restrict__ vclass, const double* __restrict__ qdense,
-                                            const double* __restrict__ qshape, const double* sq, int64_t L, int ch,
+                                            const double* __restrict__ qshape, const double* sq, IX L, int ch,
                                             int lane) {
-  const int64_t i = (int64_t)ch * 32 + lane;
-  const int64_t k = L / d.ny, j = L - k * d.ny;
-  const int64_t p = L * d.nx + i;
-  const int64_t nxy = d.nxy();
-  const double* __restrict__ w = c.xb + ((L * c.nchunks + ch) * kXBlockCoeffs) * 32 + lane;
+  const IX nx = (IX)d.nx, ny = (IX)d.ny, nz = (IX)d.nz;
+  const IX i = (IX)ch * 32 + lane;
+  const IX k = L / ny, j = L - k * ny;
+  const IX p = L * nx + i;
+  const IX nxy = nx * ny;
+  const double* __restrict__ w = c.xb + ((L * (IX)c.nchunks + ch) * kXBlockCoeffs) * 32 + lane;
   const double t = T[p];
   const double txl = i > 0 ? T[p - 1] : t;
-  const double txh = i + 1 < d.nx ? T[p + 1] : t;
-  const double tyl = j > 0 ? T[p - d.nx] : t;
-  const double tyh = j + 1 < d.ny ? T[p + d.nx] : t;
+  const double txh = i + 1 < nx ? T[p + 1] : t;
+  const double tyl = j > 0 ? T[p - nx] : t;
+  const double tyh = j + 1 < ny ? T[p + nx] : t;
   const double tzl = k > 0 ? T[p - nxy] : t;
-  const double tzh = k + 1 < d.nz ? T[p + nxy] : t;
+  const double tzh = k + 1 < nz ? T[p + nxy] : t;
   double r = w[kWc * 32] * t;
   r = fma(w[kWxl * 32], txl, r);
   r = fma(w[kWxh * 32], txh, r);
@@ -86,16 +89,17 @@ __device__ __forceinline__ double stencil_x(const Dims& d, const double* __restr
 // how long a small launch takes).
 // PITCH 0: W0 shares T's row pitch nx; 1: one pad column (odd nx: pitch nx + 1, so the W0 index of voxel (L, i)
 // is its T index plus L); 2: any other pitch c.px (padding for tests).
-template <int PITCH>
-__device__ __forceinline__ int64_t w0_index(const Dims& d, const Coeffs& c, int64_t L, int64_t i) {
-  if (PITCH == 0) return L * d.nx + i;
-  if (PITCH == 1) return L * d.nx + i + L;
-  return L * c.px + i;
+template <int PITCH, typename IX = int64_t>
+__device__ __forceinline__ IX w0_index(const Dims& d, const Coeffs& c, IX L, IX i) {
+  if (PITCH == 0) return L * (IX)d.nx + i;
+  if (PITCH == 1) return L * (IX)d.nx + i + L;
+  return L * (IX)c.px + i;
 }
 
 // The class source values come from the kernel's parameter table qt, or (QROW) from the global row qrow.  The
 // kernel owns the shared arrays: sr, sa [LINES][kXChunk + 1] and sq [HS2G_MAX_CLASSES when HAS_Q].
-template <bool HAS_Q, bool RANGED, int LINES, int PITCHED, bool QROW = false, typename QT = QTable>
+template <bool HAS_Q, bool RANGED, int LINES, int PITCHED, bool QROW = false, typename QT = QTable,
+          typename IX = int64_t>
 __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __restrict__ T, const Coeffs& c,
                                              const uint8_t* __restrict__ vclass, const double* __restrict__ qdense,
                                              const double* __restrict__ qshape, const QT& qt,
@@ -112,8 +116,9 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
         sq[e] = qt.q[e];
     }
   }
-  const int64_t nlines = RANGED ? line_end : d.nz * d.ny;
-  const int64_t L0 = (RANGED ? line_begin : 0) + (int64_t)blockIdx.x * LINES;
+  const IX nx = (IX)d.nx;
+  const IX nlines = RANGED ? (IX)line_end : (IX)(d.nz * d.ny);
+  const IX L0 = (RANGED ? (IX)line_begin : 0) + (IX)blockIdx.x * LINES;
   const int nchunks = (int)((d.nx + kXChunk - 1) / kXChunk);
   wait_prior_grid();  // T comes from the previous step's z sweep, which used W0 as its scratch
   __syncthreads();
@@ -121,15 +126,15 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
   // forward: z_i = R'_i - a0_i * z_{i-1}
   double carry = 0.0;
   for (int ch = 0; ch < nchunks; ++ch) {
-    const int64_t i = (int64_t)ch * kXChunk + lane;
+    const IX i = (IX)ch * kXChunk + lane;
 #pragma unroll
     for (int ll = 0; ll < kPerWarp; ++ll) {
       const int l = warp * kPerWarp + ll;
-      const int64_t L = L0 + l;
+      const IX L = L0 + l;
       double r = 0.0, a = 0.0;
-      if (L < nlines && i < d.nx) {
-        r = stencil_x<HAS_Q>(d, T, c, vclass, qdense, qshape, sq, L, ch, lane);
-        a = c.a0[L * d.nx + i];
+      if (L < nlines && i < nx) {
+        r = stencil_x<HAS_Q, IX>(d, T, c, vclass, qdense, qshape, sq, L, ch, lane);
+        a = c.a0[L * nx + i];
       }
       sr[l][lane] = r;
       sa[l][lane] = a;
@@ -149,8 +154,8 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
 #pragma unroll
     for (int ll = 0; ll < kPerWarp; ++ll) {
       const int l = warp * kPerWarp + ll;
-      const int64_t L = L0 + l;
-      if (L < nlines && i < d.nx) W0[w0_index<PITCHED>(d, c, L, i)] = sr[l][lane];
+      const IX L = L0 + l;
+      if (L < nlines && i < nx) W0[w0_index<PITCHED, IX>(d, c, L, i)] = sr[l][lane];
     }
     __syncthreads();
   }
@@ -158,15 +163,15 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
   // back substitution: W0_i = z_i - b0_i * W0_{i+1}
   carry = 0.0;
   for (int ch = nchunks - 1; ch >= 0; --ch) {
-    const int64_t i = (int64_t)ch * kXChunk + lane;
+    const IX i = (IX)ch * kXChunk + lane;
 #pragma unroll
     for (int ll = 0; ll < kPerWarp; ++ll) {
       const int l = warp * kPerWarp + ll;
-      const int64_t L = L0 + l;
+      const IX L = L0 + l;
       double z = 0.0, b = 0.0;
-      if (L < nlines && i < d.nx) {
-        const int64_t p = L * d.nx + i;
-        z = W0[w0_index<PITCHED>(d, c, L, i)];
+      if (L < nlines && i < nx) {
+        const IX p = L * nx + i;
+        z = W0[w0_index<PITCHED, IX>(d, c, L, i)];
         b = c.b0[p];
       }
       sr[l][lane] = z;
@@ -187,8 +192,8 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
 #pragma unroll
     for (int ll = 0; ll < kPerWarp; ++ll) {
       const int l = warp * kPerWarp + ll;
-      const int64_t L = L0 + l;
-      if (L < nlines && i < d.nx) W0[w0_index<PITCHED>(d, c, L, i)] = sr[l][lane];
+      const IX L = L0 + l;
+      if (L < nlines && i < nx) W0[w0_index<PITCHED, IX>(d, c, L, i)] = sr[l][lane];
     }
     __syncthreads();
   }
@@ -203,7 +208,7 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
 // every launch for nothing).
 template <bool HAS_Q>
 using XTable = typename std::conditional<HAS_Q, QTable, int>::type;
-template <bool HAS_Q, bool RANGED, int LINES, int PITCH>
+template <bool HAS_Q, bool RANGED, int LINES, int PITCH, typename IX = int64_t>
 __global__ void __maxnreg__(72) sweep_x_lean_kernel(Dims d, const double* __restrict__ T, Coeffs c,
                                                     const uint8_t* __restrict__ vclass,
                                                     const double* __restrict__ qdense,
@@ -212,8 +217,8 @@ __global__ void __maxnreg__(72) sweep_x_lean_kernel(Dims d, const double* __rest
   __shared__ double sr[LINES][kXChunk + 1];
   __shared__ double sa[LINES][kXChunk + 1];
   __shared__ double sq[HAS_Q ? HS2G_MAX_CLASSES : 1];
-  sweep_x_body<HAS_Q, RANGED, LINES, PITCH>(d, T, c, vclass, qdense, qshape, qt, nullptr, W0, line_begin, line_end,
-                                            sr, sa, sq);
+  sweep_x_body<HAS_Q, RANGED, LINES, PITCH, false, XTable<HAS_Q>, IX>(d, T, c, vclass, qdense, qshape, qt, nullptr,
+                                                                      W0, line_begin, line_end, sr, sa, sq);
 }
 // The line ranges of the host-buffer step on unpadded rows keep the 6-block bound (80 registers at 32 lines per
 // CTA): measured against the 72-register build there, 9.62e9 against 9.39e9 voxel-steps/s end to end.
@@ -255,6 +260,17 @@ __global__ void __maxnreg__(72) sweep_x_row_kernel(Dims d, const double* __restr
                                                   sa, sq);
 }
 
+// Whether the whole-grid x sweep may index in 32 bits: every voxel index (with the pad column of an odd nx) and
+// every stencil-block element below 2^31.  HS2G_X_INDEX=64 keeps 64-bit indices.
+bool x_index32(const Dims& d, const Coeffs& c) {
+  static const bool off = [] {
+    const char* e = getenv("HS2G_X_INDEX");
+    return e && strcmp(e, "64") == 0;
+  }();
+  const int64_t lim = (int64_t)1 << 31;
+  return !off && d.nvox() + d.nz * d.ny < lim && d.nz * d.ny * c.nchunks * kXBlockCoeffs * 32 < lim;
+}
+
 // x sweep over all lines (RANGED false) or the lines [line_begin, line_end) of the host-buffer step
 template <bool RANGED, int LINES>
 void launch_x(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_begin, int64_t line_end,
@@ -266,6 +282,22 @@ void launch_x(const StepArgs& a, const Coeffs& c, const QTable& q, int64_t line_
 #define HS2G_X(KERNEL, TABLE, ...)                                                                             \
   launch_kernel(KERNEL<__VA_ARGS__>, dim3(gx), dim3(kXThreads), 0, s, a.pdl_x, d, a.T_in, c, a.vclass, a.qdense, \
                 a.qshape, TABLE, a.W0, line_begin, line_end)
+  if constexpr (!RANGED) {
+    if (pitch < 2 && x_index32(d, c)) {
+      if (pitch == 0) {
+        if (has_q)
+          HS2G_X(sweep_x_lean_kernel, q, true, false, LINES, 0, int32_t);
+        else
+          HS2G_X(sweep_x_lean_kernel, 0, false, false, LINES, 0, int32_t);
+      } else {
+        if (has_q)
+          HS2G_X(sweep_x_lean_kernel, q, true, false, LINES, 1, int32_t);
+        else
+          HS2G_X(sweep_x_lean_kernel, 0, false, false, LINES, 1, int32_t);
+      }
+      return;
+    }
+  }
   if (RANGED && pitch == 0) {
     if (has_q)
       HS2G_X(sweep_x_kernel, q, true, RANGED, LINES);
