@@ -144,9 +144,17 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
       const int l = warp * 32 + lane;
       const int cw = (int)min((int64_t)kXChunk, d.nx - (int64_t)ch * kXChunk);
       double z = carry;
-      for (int cc = 0; cc < cw; ++cc) {
-        z = fma(-sa[l][cc], z, sr[l][cc]);
-        sr[l][cc] = z;
+      if (cw == kXChunk) {  // full chunks unrolled: the shared loads of later rows issue ahead of the chain
+#pragma unroll 8
+        for (int cc = 0; cc < kXChunk; ++cc) {
+          z = fma(-sa[l][cc], z, sr[l][cc]);
+          sr[l][cc] = z;
+        }
+      } else {
+        for (int cc = 0; cc < cw; ++cc) {
+          z = fma(-sa[l][cc], z, sr[l][cc]);
+          sr[l][cc] = z;
+        }
       }
       carry = z;
     }
@@ -182,9 +190,17 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
       const int l = warp * 32 + lane;
       const int cw = (int)min((int64_t)kXChunk, d.nx - (int64_t)ch * kXChunk);
       double x = carry;
-      for (int cc = cw - 1; cc >= 0; --cc) {
-        x = fma(-sa[l][cc], x, sr[l][cc]);
-        sr[l][cc] = x;
+      if (cw == kXChunk) {
+#pragma unroll 8
+        for (int cc = kXChunk - 1; cc >= 0; --cc) {
+          x = fma(-sa[l][cc], x, sr[l][cc]);
+          sr[l][cc] = x;
+        }
+      } else {
+        for (int cc = cw - 1; cc >= 0; --cc) {
+          x = fma(-sa[l][cc], x, sr[l][cc]);
+          sr[l][cc] = x;
+        }
       }
       carry = x;
     }
