@@ -145,7 +145,7 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
       const int cw = (int)min((int64_t)kXChunk, d.nx - (int64_t)ch * kXChunk);
       double z = carry;
       if (cw == kXChunk) {  // full chunks unrolled: the shared loads of later rows issue ahead of the chain
-#pragma unroll 8
+#pragma unroll 4
         for (int cc = 0; cc < kXChunk; ++cc) {
           z = fma(-sa[l][cc], z, sr[l][cc]);
           sr[l][cc] = z;
@@ -191,7 +191,7 @@ __device__ __forceinline__ void sweep_x_body(const Dims& d, const double* __rest
       const int cw = (int)min((int64_t)kXChunk, d.nx - (int64_t)ch * kXChunk);
       double x = carry;
       if (cw == kXChunk) {
-#pragma unroll 8
+#pragma unroll 4
         for (int cc = kXChunk - 1; cc >= 0; --cc) {
           x = fma(-sa[l][cc], x, sr[l][cc]);
           sr[l][cc] = x;
