@@ -68,24 +68,27 @@ struct BatchView {
 
 constexpr int kMaxBatchClasses = HS2G_MAX_CLASSES;
 
-template <typename R, bool HAS_Q>
+// IX: index type of the voxel, line and stencil-block arithmetic within an instance (int32_t when every
+// instance and its stencil blocks have fewer than 2^31 elements)
+template <typename R, bool HAS_Q, typename IX = int64_t>
 __device__ __forceinline__ R batch_stencil(const Inst& I, const R* __restrict__ T, const R* __restrict__ xb,
-                                           const uint8_t* __restrict__ vclass, const R* sq, int64_t L, int ch,
+                                           const uint8_t* __restrict__ vclass, const R* sq, IX L, int ch,
                                            int lane) {
   const Dims& d = I.d;
-  const int64_t i = (int64_t)ch * 32 + lane;
-  const int64_t k = L / d.ny, j = L - k * d.ny;
-  const int64_t p = L * d.nx + i;
-  const int64_t nxy = d.nxy();
-  const R* __restrict__ w = xb + I.xb_off + ((L * I.nchunks + ch) * kXBlockCoeffs) * 32 + lane;
+  const IX nx = (IX)d.nx, ny = (IX)d.ny, nz = (IX)d.nz;
+  const IX i = (IX)ch * 32 + lane;
+  const IX k = L / ny, j = L - k * ny;
+  const IX p = L * nx + i;
+  const IX nxy = nx * ny;
+  const R* __restrict__ w = xb + I.xb_off + ((L * (IX)I.nchunks + ch) * kXBlockCoeffs) * 32 + lane;
   const R* Ti = T + I.off;
   const R t = Ti[p];
   const R txl = i > 0 ? Ti[p - 1] : t;
-  const R txh = i + 1 < d.nx ? Ti[p + 1] : t;
-  const R tyl = j > 0 ? Ti[p - d.nx] : t;
-  const R tyh = j + 1 < d.ny ? Ti[p + d.nx] : t;
+  const R txh = i + 1 < nx ? Ti[p + 1] : t;
+  const R tyl = j > 0 ? Ti[p - nx] : t;
+  const R tyh = j + 1 < ny ? Ti[p + nx] : t;
   const R tzl = k > 0 ? Ti[p - nxy] : t;
-  const R tzh = k + 1 < d.nz ? Ti[p + nxy] : t;
+  const R tzh = k + 1 < nz ? Ti[p + nxy] : t;
   R r = w[kWc * 32] * t;
   r = fma(w[kWxl * 32], txl, r);
   r = fma(w[kWxh * 32], txh, r);
@@ -98,27 +101,28 @@ __device__ __forceinline__ R batch_stencil(const Inst& I, const R* __restrict__ 
 }
 
 // One block of 32 x-lines of one instance (CTA of 128 threads), same structure as sweep_x_kernel.
-template <typename R, bool HAS_Q>
-__device__ void batch_x_block(const BatchView<R>& v, const Inst& I, int64_t L0, const R* sq, R (*sr)[33],
+template <typename R, bool HAS_Q, typename IX = int64_t>
+__device__ void batch_x_block(const BatchView<R>& v, const Inst& I, int64_t L0_, const R* sq, R (*sr)[33],
                               R (*sa)[33]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const Dims& d = I.d;
-  const int64_t nlines = d.nz * d.ny;
+  const IX nx = (IX)d.nx, L0 = (IX)L0_;
+  const IX nlines = (IX)(d.nz * d.ny);
   const int nchunks = (int)I.nchunks;
   R* W0 = v.W0 + I.off;
   const R* a0 = v.a0 + I.off;
   const R* b0 = v.b0 + I.off;
   R carry = 0;
   for (int ch = 0; ch < nchunks; ++ch) {
-    const int64_t i = (int64_t)ch * 32 + lane;
+    const IX i = (IX)ch * 32 + lane;
 #pragma unroll
     for (int ll = 0; ll < 8; ++ll) {
       const int l = warp * 8 + ll;
-      const int64_t L = L0 + l;
+      const IX L = L0 + l;
       R r = 0, a = 0;
-      if (L < nlines && i < d.nx) {
-        r = batch_stencil<R, HAS_Q>(I, v.T, v.xb, v.vclass, sq, L, ch, lane);
-        a = a0[L * d.nx + i];
+      if (L < nlines && i < nx) {
+        r = batch_stencil<R, HAS_Q, IX>(I, v.T, v.xb, v.vclass, sq, L, ch, lane);
+        a = a0[L * nx + i];
       }
       sr[l][lane] = r;
       sa[l][lane] = a;
@@ -137,22 +141,22 @@ __device__ void batch_x_block(const BatchView<R>& v, const Inst& I, int64_t L0, 
 #pragma unroll
     for (int ll = 0; ll < 8; ++ll) {
       const int l = warp * 8 + ll;
-      const int64_t L = L0 + l;
-      if (L < nlines && i < d.nx) W0[L * d.nx + i] = sr[l][lane];
+      const IX L = L0 + l;
+      if (L < nlines && i < nx) W0[L * nx + i] = sr[l][lane];
     }
     __syncthreads();
   }
   carry = 0;
   for (int ch = nchunks - 1; ch >= 0; --ch) {
-    const int64_t i = (int64_t)ch * 32 + lane;
+    const IX i = (IX)ch * 32 + lane;
 #pragma unroll
     for (int ll = 0; ll < 8; ++ll) {
       const int l = warp * 8 + ll;
-      const int64_t L = L0 + l;
+      const IX L = L0 + l;
       R z = 0, b = 0;
-      if (L < nlines && i < d.nx) {
-        z = W0[L * d.nx + i];
-        b = b0[L * d.nx + i];
+      if (L < nlines && i < nx) {
+        z = W0[L * nx + i];
+        b = b0[L * nx + i];
       }
       sr[l][lane] = z;
       sa[l][lane] = b;
@@ -171,8 +175,8 @@ __device__ void batch_x_block(const BatchView<R>& v, const Inst& I, int64_t L0, 
 #pragma unroll
     for (int ll = 0; ll < 8; ++ll) {
       const int l = warp * 8 + ll;
-      const int64_t L = L0 + l;
-      if (L < nlines && i < d.nx) W0[L * d.nx + i] = sr[l][lane];
+      const IX L = L0 + l;
+      if (L < nlines && i < nx) W0[L * nx + i] = sr[l][lane];
     }
     __syncthreads();
   }
@@ -180,7 +184,7 @@ __device__ void batch_x_block(const BatchView<R>& v, const Inst& I, int64_t L0, 
 
 // 72 registers (7 CTAs of 128 threads per SM): more loads in flight per thread than at 64 registers, which
 // left the kernel load-latency bound (2.25e10 against 2.47e10 voxel-steps/s on the 256-instance batch).
-template <typename R>
+template <typename R, typename IX = int64_t>
 __global__ void __launch_bounds__(128, 7) batch_x_kernel(BatchView<R> v) {
   __shared__ R sr[32][33];
   __shared__ R sa[32][33];
@@ -195,9 +199,9 @@ __global__ void __launch_bounds__(128, 7) batch_x_kernel(BatchView<R> v) {
       const R* q = v.qtabs + ((int64_t)step * v.ninst + item.inst) * v.nclass;
       for (int c = threadIdx.x; c < kMaxBatchClasses; c += blockDim.x) sq[c] = c < v.nclass ? q[c] : R(0);
       __syncthreads();
-      batch_x_block<R, true>(v, I, item.L0, sq, sr, sa);
+      batch_x_block<R, true, IX>(v, I, item.L0, sq, sr, sa);
     } else {
-      batch_x_block<R, false>(v, I, item.L0, sq, sr, sa);
+      batch_x_block<R, false, IX>(v, I, item.L0, sq, sr, sa);
     }
   }
 }
@@ -315,6 +319,7 @@ struct Batch {
   LWork* zw = nullptr;
   int64_t nxw = 0, nyw = 0, nzw = 0;
   Tuning tune{0, 128, 0, 128, 0};
+  bool ix32 = false;  // every instance's voxels and stencil blocks below 2^31 elements: 32-bit x-sweep indices
   cudaGraphExec_t graph = nullptr;
   int64_t bytes = 0;
   size_t elem() const { return precision == 64 ? 8 : 4; }
@@ -357,7 +362,10 @@ template <typename R>
 cudaError_t launch_axis(const Batch& b, int axis, const Tuning& t, cudaStream_t s) {
   BatchView<R> v = view<R>(b);
   if (axis == 0) {
-    batch_x_kernel<R><<<(unsigned)std::max(1, t.x_grid), 128, 0, s>>>(v);
+    if (b.ix32)
+      batch_x_kernel<R, int32_t><<<(unsigned)std::max(1, t.x_grid), 128, 0, s>>>(v);
+    else
+      batch_x_kernel<R><<<(unsigned)std::max(1, t.x_grid), 128, 0, s>>>(v);
   } else if (axis == 1) {
     batch_y_kernel<R><<<(unsigned)std::max(1, t.y_grid), t.y_block, 0, s>>>(v);
   } else if (axis == 2) {
@@ -719,6 +727,9 @@ int hs2g_batch_create(int n, const hs2g_class_problem* problems, int precision, 
   }
   b.nvox = off;
   b.xb_len = xoff;
+  b.ix32 = true;
+  for (const hs2g::Inst& I : b.inst)
+    b.ix32 = b.ix32 && I.d.nvox() < ((int64_t)1 << 31) && xb_elems(I.d) < ((int64_t)1 << 31);
   const size_t el = b.elem();
   double* wsp = nullptr;
   unsigned long long* err = nullptr;
