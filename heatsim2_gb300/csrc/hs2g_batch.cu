@@ -131,9 +131,17 @@ __device__ void batch_x_block(const BatchView<R>& v, const Inst& I, int64_t L0_,
     if (warp == 0) {
       const int cw = (int)min((int64_t)32, d.nx - (int64_t)ch * 32);
       R z = carry;
-      for (int cc = 0; cc < cw; ++cc) {
-        z = fma(-sa[lane][cc], z, sr[lane][cc]);
-        sr[lane][cc] = z;
+      if (cw == 32) {  // full chunks unrolled: the shared loads of later rows issue ahead of the chain
+#pragma unroll 4
+        for (int cc = 0; cc < 32; ++cc) {
+          z = fma(-sa[lane][cc], z, sr[lane][cc]);
+          sr[lane][cc] = z;
+        }
+      } else {
+        for (int cc = 0; cc < cw; ++cc) {
+          z = fma(-sa[lane][cc], z, sr[lane][cc]);
+          sr[lane][cc] = z;
+        }
       }
       carry = z;
     }
@@ -165,9 +173,17 @@ __device__ void batch_x_block(const BatchView<R>& v, const Inst& I, int64_t L0_,
     if (warp == 0) {
       const int cw = (int)min((int64_t)32, d.nx - (int64_t)ch * 32);
       R x = carry;
-      for (int cc = cw - 1; cc >= 0; --cc) {
-        x = fma(-sa[lane][cc], x, sr[lane][cc]);
-        sr[lane][cc] = x;
+      if (cw == 32) {
+#pragma unroll 4
+        for (int cc = 31; cc >= 0; --cc) {
+          x = fma(-sa[lane][cc], x, sr[lane][cc]);
+          sr[lane][cc] = x;
+        }
+      } else {
+        for (int cc = cw - 1; cc >= 0; --cc) {
+          x = fma(-sa[lane][cc], x, sr[lane][cc]);
+          sr[lane][cc] = x;
+        }
       }
       carry = x;
     }
