@@ -510,11 +510,17 @@ __global__ void __launch_bounds__(64) adj_ysolve_few_kernel(AView v, int axis, i
   for (int q = 0; q < nq; ++q) {
     named_bar_sync(1 + q % kFS, 64);
     if (q < nb) {
+      double ce[kFR], cc[kFR];  // the block's operands in registers before the chain (no wait behind its stores)
+#pragma unroll
+      for (int k = 0; k < kFR; ++k) {
+        ce[k] = *R.at(q, k, 1);
+        cc[k] = *R.at(q, k, 0);
+      }
 #pragma unroll
       for (int k = 0; k < kFR; ++k) {
         const int r = q * kFR + k;
         if (r < len) {
-          z = __fma_rn(-*R.at(q, k, 1), z, *R.at(q, k, 0));
+          z = __fma_rn(-ce[k], z, cc[k]);
           line[r * 32 + lane] = z;
         }
       }
