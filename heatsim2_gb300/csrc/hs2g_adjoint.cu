@@ -637,8 +637,22 @@ __global__ void __launch_bounds__(128) adj_xsolve_few_kernel(AView v, int64_t ma
         zr[cc] = z;
       };
       if (cw == kXC) {
-#pragma unroll 8
-        for (int cc = 0; cc < kXC; ++cc) step(cc);
+        // eight columns' operands in registers before their part of the chain (the loads do not wait behind the
+        // chain's stores to the line buffer)
+#pragma unroll
+        for (int c0 = 0; c0 < kXC; c0 += 8) {
+          double ee[8], c8[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            ee[u] = te[c0 + u];
+            c8[u] = tc[c0 + u];
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            z = __fma_rn(-ee[u], z, c8[u]);
+            zr[c0 + u] = z;
+          }
+        }
       } else {
         for (int cc = 0; cc < cw; ++cc) step(cc);
       }
@@ -663,8 +677,20 @@ __global__ void __launch_bounds__(128) adj_xsolve_few_kernel(AView v, int64_t ma
         zr[cc] = x;
       };
       if (cw == kXC) {
-#pragma unroll 8
-        for (int cc = kXC - 1; cc >= 0; --cc) step(cc);
+#pragma unroll
+        for (int c1 = kXC - 1; c1 >= 0; c1 -= 8) {  // eight columns' operands in registers first
+          double u8[8], z8[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            u8[u] = tu[c1 - u];
+            z8[u] = zr[c1 - u];
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            x = __fma_rn(-u8[u], x, z8[u]);
+            zr[c1 - u] = x;
+          }
+        }
       } else {
         for (int cc = cw - 1; cc >= 0; --cc) step(cc);
       }
