@@ -22,7 +22,7 @@ def golden_files(include_big=True, curved=False):
     out = []
     for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
         b = os.path.basename(f)
-        if b.startswith("stages_") or b in ("tridiag.npz", "surface_temperature.npz"):
+        if b.startswith("stages_") or b in ("tridiag.npz", "surface_temperature.npz", "uneven_batch_sample.npz"):
             continue
         if b.startswith("curved_") != curved:
             continue
@@ -50,6 +50,26 @@ def load_golden(path):
         elif not k.endswith("_nz"):
             steps[int(k[2:])] = np.array(z[k])
     return spec, [float(t) for t in z["times"]], steps
+
+
+def load_uneven_sample():
+    """The reference's outputs for instances 0 and 2 of the benchmark's uneven batch (tests/golden/make_golden.py
+    uneven): {instance: (spec, times, {"top_1", "top_10", "xz_10", "yz_10"})} -- the top plane after steps 1 and
+    10 and the x-z / y-z slices through the middle of the grid after step 10."""
+    from heatsim2_gb300 import workloads as W
+    z = np.load(os.path.join(GOLDEN, "uneven_batch_sample.npz"))
+    out = {}
+    for n in (int(v) for v in z["instances"]):
+        spec = W.spec_from_npz(z, prefix="i%d_spec_" % n)
+        ref = {k: np.array(z["i%d_%s" % (n, k)]) for k in ("top_1", "top_10", "xz_10", "yz_10")}
+        out[n] = (spec, [float(t) for t in z["i%d_times" % n]], ref)
+    return out
+
+
+def uneven_sample_slices(T):
+    """The slices of a field that the uneven-batch fixture stores: top plane, middle x-z and y-z slices."""
+    nz, ny, nx = T.shape
+    return {"top": T[0], "xz": T[:, ny // 2, :], "yz": T[:, :, nx // 2]}
 
 
 def rel_err(a, ref):

@@ -3,7 +3,8 @@
 Run in a container where the reference sources are mounted (the reference is built into oracle/_ref by
 oracle/build_ref.py first):
 
-    python oracle/build_ref.py && python tests/golden/make_golden.py [curved | surface | composite128 | unaligned]
+    python oracle/build_ref.py && python tests/golden/make_golden.py [curved | surface | composite128 | uneven |
+        unaligned]
 
 Each fixture ``<name>.npz`` holds the problem spec (heatsim2_gb300.workloads serialisation), the t values
 passed to the reference's run_adi_steps, and the temperature field the reference returned after selected
@@ -129,6 +130,30 @@ def composite_panel_128(hs):
     print("wrote composite_panel_128")
 
 
+def uneven_batch_sample(hs):
+    """Instances 0 (steel slab, 57 x 114 x 85) and 2 (composite panel, 60 x 74 x 171) of the 256-instance
+    uneven batch the benchmark runs (seed 2), 10 steps of the reference each.  Stored per instance: the spec, the
+    top plane after step 1 and, after step 10, the top plane and the x-z and y-z slices through the middle of the
+    grid (the whole fields would make the fixture megabytes)."""
+    specs = W.uneven_batch(seed=2, n=3, nsteps=10)
+    d = {"instances": np.array([0, 2])}
+    for n in (0, 2):
+        spec = specs[n]
+        _, _, times, res = run_reference(hs, spec, {1, 10})
+        for key, val in W.spec_to_npz_dict(spec).items():
+            d["i%d_%s" % (n, key)] = val
+        d["i%d_times" % n] = np.array(times)
+        T1, T10 = res["T_1"], res["T_10"]
+        nz, ny, nx = T10.shape
+        d["i%d_top_1" % n] = np.ascontiguousarray(T1[0])
+        d["i%d_top_10" % n] = np.ascontiguousarray(T10[0])
+        d["i%d_xz_10" % n] = np.ascontiguousarray(T10[:, ny // 2, :])
+        d["i%d_yz_10" % n] = np.ascontiguousarray(T10[:, :, nx // 2])
+        print("instance", n, T10.shape, "max |T - 293| %.3g" % np.abs(T10 - 293.0).max())
+    np.savez_compressed(os.path.join(HERE, "uneven_batch_sample.npz"), **d)
+    print("wrote uneven_batch_sample")
+
+
 def unaligned_fixture(hs):
     """What the reference's setup does with unaligned_anisotropic=True (alternatingdirection_c_pyx.pyx:511-564,
     crank_nicolson.pyx:140-143) on a tensor aligned with the axes, an unaligned tensor and a scalar-k slab with
@@ -171,6 +196,9 @@ def main():
     if len(sys.argv) > 1 and sys.argv[1] == "surface":
         surface_fixture(hs)
         return
+    if len(sys.argv) > 1 and sys.argv[1] == "uneven":
+        uneven_batch_sample(hs)
+        return
     import heatsim2.tridiag as ref_tridiag
     tridiag_fixture(ref_tridiag)
 
@@ -186,6 +214,7 @@ def main():
     curved_fixtures(hs)
     surface_fixture(hs)
     composite_panel_128(hs)
+    uneven_batch_sample(hs)
     unaligned_fixture(hs)
 
 

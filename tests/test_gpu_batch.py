@@ -4,7 +4,7 @@ stays within its stated error of FP64."""
 import numpy as np
 import pytest
 
-from conftest import rel_err
+from conftest import load_uneven_sample, rel_err, uneven_sample_slices
 import oracle
 from oracle_shim import HS
 import heatsim2_gb300 as hs
@@ -107,3 +107,29 @@ def test_benchmark_batch_instances_vs_oracle(cuda_ok):
     print("batch vs oracle: FP64 %.2e, FP32 %.2e" % (worst64, worst32))
     assert worst64 <= 1e-12, worst64
     assert worst32 <= 1e-7, worst32
+
+
+def test_benchmark_batch_instances_vs_reference(cuda_ok):
+    """Instances 0 and 2 of the benchmark's 256-instance uneven batch (57x114x85 steel slab, 60x74x171 composite
+    panel: odd row widths), advanced together in one batched state and compared with the reference's own output
+    (tests/golden/uneven_batch_sample.npz): the top plane after step 1 and, after step 10, the top plane and the
+    x-z / y-z slices through the middle of each grid.  FP64 within 1e-12 of max|T|, FP32 within 1e-7."""
+    sample = load_uneven_sample()
+    specs = [sample[n][0] for n in sorted(sample)]
+    times = sample[min(sample)][1]
+    assert all(sample[n][1] == times for n in sample)     # one source schedule for the batch
+    for precision, tol in ((64, 1e-12), (32, 1e-7)):
+        b = Batch([W.setup_args(hs, s) for s in specs], precision=precision)
+        b.set_temperature([W.initial_temperature(s) for s in specs])
+        b.set_sources(times, specs[0]["dt"])
+        b.run(1)
+        worst = 0.0
+        for n, T in zip(sorted(sample), b.get_temperature()):
+            worst = max(worst, rel_err(T[0], sample[n][2]["top_1"]))
+        b.run(len(times) - 1)
+        for n, T in zip(sorted(sample), b.get_temperature()):
+            sl = uneven_sample_slices(T)
+            for key in ("top", "xz", "yz"):
+                worst = max(worst, rel_err(sl[key], sample[n][2][key + "_10"]))
+        print("batch FP%d vs reference: %.2e" % (precision, worst))
+        assert worst <= tol, (precision, worst)

@@ -6,7 +6,7 @@ every fixture; the tolerance allows 1e-14 to stay robust to compiler contraction
 import numpy as np
 import pytest
 
-from conftest import golden_files, load_golden, rel_err, GOLDEN
+from conftest import golden_files, load_golden, load_uneven_sample, rel_err, uneven_sample_slices, GOLDEN
 
 import oracle
 from oracle_shim import HS  # noqa: F401  (module-like names for the oracle)
@@ -23,6 +23,22 @@ def test_oracle_matches_reference(path):
         T = oracle.run_adi_steps(P, None, t, spec["dt"], T, spec["arrays"]["volumetric"], vol)
         if n + 1 in ref:
             assert rel_err(T, ref[n + 1]) <= 1e-14, (n + 1)
+
+
+def test_oracle_matches_reference_on_benchmark_batch_instances():
+    """Instances 0 and 2 of the benchmark's 256-instance uneven batch (a 57x114x85 steel slab and a 60x74x171
+    composite panel, odd row widths), 10 steps: the oracle reproduces the reference's stored planes and slices."""
+    for n, (spec, times, ref) in load_uneven_sample().items():
+        P, _ = oracle.setup(*W.setup_args(HS, spec))
+        vol = W.volumetric_tuple(HS, spec)
+        T = W.initial_temperature(spec)
+        for k, t in enumerate(times):
+            T = oracle.run_adi_steps(P, None, t, spec["dt"], T, spec["arrays"]["volumetric"], vol)
+            if k == 0:
+                assert rel_err(T[0], ref["top_1"]) <= 1e-14, n
+        sl = uneven_sample_slices(T)
+        for key in ("top", "xz", "yz"):
+            assert rel_err(sl[key], ref[key + "_10"]) <= 1e-14, (n, key)
 
 
 def test_oracle_tridiag_matches_reference():
